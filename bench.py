@@ -1,0 +1,380 @@
+"""Benchmark of the nls time-stepping path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+One bench step = one complete solve of the workload: by default the batched form, 512 independent
+solves (256 radial grids of 500-8192 nodes, 256 square grids of 64-512 per side; seeded
+synthetic inputs) advanced 5000 RK4 steps each in complex64 by one graph-captured launch
+sequence.  Throughput is node-steps/s (one node-step = one grid point advanced one full RK4
+step).  The line also carries the plain complex128 GPU path on a sample of the same instances,
+the relative L2 error of |psi|^2 and of the reservoir n against complex128 solves, a short
+served stream (p50/p99), the roofline of the fused 2-D step kernel, the CPU oracle timed on the
+host cores, the end-to-end figure through the host-buffer C ABI, and the SM clocks sampled
+during the timed region.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "node-steps/s batched FP32 vs plain FP64 GPU at relL2≤1e-4; serve p50/p99 ms"
+UNIT = "node-steps/s"
+SOLVE_STEPS = 5000
+# Algorithmic HBM bytes per node-step of the fused single-pass 2-D step (complex64 state read and
+# written once, float32 pump read once): 8 + 4 + 8.
+BYTES_PER_NODE_STEP_C64 = 20
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_per_node():
+    """DRAM bytes per node per fused-step launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "rk4_2d_fused_c64_batch_mix.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_node_step:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, value: float, device) -> float:
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU oracle leg
+
+def cpu_oracle_rate(specs, steps, threads):
+    """node-steps/s of the float32 oracle (the reference algorithm, C++ restatement) over specs."""
+    from oracle import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    ns = 0
+    for s in specs:
+        oracle.solve(s.dt, s.dx, s.order, steps, s.pumping, s.coeffs, s.u0, dtype=np.float32,
+                     threads=threads if s.dim == 2 else 1)
+        ns += s.nodes * steps
+    dt = time.perf_counter() - t0
+    return ns / dt, dt
+
+
+def oracle_sample(specs):
+    """Bounded sample of the mix for the CPU leg: every 4th instance of each kind."""
+    return [s for i, s in enumerate(specs) if i % 4 == 0]
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm on the host cores (the oracle port), same metric."""
+    ws, rank, local = dist_init()
+    if rank != 0:
+        return 0
+    from nls_gb300 import workloads
+    specs = oracle_sample(workloads.batch_mix())
+    threads = os.cpu_count() or 1
+    steps = 4
+    for _ in range(args.warmup):
+        cpu_oracle_rate(specs[:8], 1, threads)
+    rates, times = [], []
+    for _ in range(args.steps):
+        r, t = cpu_oracle_rate(specs, steps, threads)
+        rates.append(r)
+        times.append(t)
+    value = float(np.mean(rates))
+    sample = f"every 4th of the 512 mixed instances ({len(specs)} solves), {steps} RK4 steps each, float32"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times) * 1e3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "batch_mix", "instances": 512, "steps_per_solve": SOLVE_STEPS},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's Fortran cannot be compiled here (no Fortran compiler); the oracle's C++ "
+                "restatement of nls/nls.f90 is timed instead",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU legs
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_init()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    from nls_gb300 import build as nbuild
+    nbuild.build()
+    from nls_gb300 import device as ndev
+    from nls_gb300 import workloads
+    from nls_gb300.batch import BatchSolver
+    from nls_gb300.native import nls
+
+    specs = workloads.batch_mix()
+    total_nodes = sum(s.nodes for s in specs)
+    nodes_2d = sum(s.nodes for s in specs if s.dim == 2)
+    b = BatchSolver(specs, dtype=np.complex64, device=local)
+    ext = ndev.stream(local)
+
+    # warm-up: includes graph capture/instantiation for SOLVE_STEPS
+    for _ in range(args.warmup):
+        b.run(SOLVE_STEPS)
+    b.synchronize()
+
+    launches0 = ndev.launches(local)
+    barrier(ws)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(ext)
+        for _ in range(args.steps):
+            b.run(SOLVE_STEPS)
+        e1.record(ext)
+        e1.synchronize()
+    torch.cuda.synchronize(dev)
+    barrier(ws)
+    ms = e0.elapsed_time(e1)
+    gpu_launches = ndev.launches(local) - launches0
+    ms = max_over_ranks(ws, ms, dev)
+    node_steps = float(total_nodes) * SOLVE_STEPS * args.steps * ws
+    value = node_steps / (ms / 1e3)
+    clocks = clk.summary()
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "complex64", "data": "synthetic (seeded)",
+        "config": {"workload": "batch_mix: 256 radial grids (500-8192 nodes, order 5) + 256 square grids "
+                               "(64-512 per side, order 3), 5000 RK4 steps each, complex64",
+                   "instances": len(specs), "steps_per_solve": SOLVE_STEPS, "total_nodes": total_nodes,
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (2-D states + pumps ~%.0f MB per step)" %
+                         (nodes_2d * BYTES_PER_NODE_STEP_C64 / 1e6)},
+        "gpu_launches": int(gpu_launches),
+        "clocks": clocks,
+    }
+    if rank != 0:
+        return 0
+
+    # ---- roofline of the fused 2-D step kernel (the dominant kernel), timed alone on its stream
+    specs2 = [s for s in specs if s.dim == 2]
+    b2 = BatchSolver(specs2, dtype=np.complex64, device=local)
+    L = 200
+    b2.run(L)
+    b2.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(ext)
+    b2.run(L)
+    f1.record(ext)
+    f1.synchronize()
+    launch_s = f0.elapsed_time(f1) / 1e3 / L
+    alg_bytes = BYTES_PER_NODE_STEP_C64 * nodes_2d
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / launch_s / 1e9
+    tpn = _traffic_per_node()
+    result["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                          "frac": achieved / peak, "traffic": (tpn * nodes_2d if tpn else None),
+                          "kernel": "rk4_2d_fused<float,K=1,64x64> over all 2-D tiles, one launch per RK4 step",
+                          "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": launch_s * 1e6,
+                          "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"}
+    b2.close()
+
+    # ---- accuracy of the batched complex64 results and the plain complex128 path on a sample
+    sample_idx = list(range(0, 256, 32)) + list(range(256, 512, 32))
+    import torch as T
+    errs_d, errs_n = [], []
+    plain_ns, plain_s = 0.0, 0.0
+    # a fresh batch of the sample: exactly SOLVE_STEPS steps from u0
+    bs = BatchSolver([specs[i] for i in sample_idx], dtype=np.complex64, device=local)
+    bs.run(SOLVE_STEPS)
+    bs.synchronize()
+    for k, i in enumerate(sample_idx):
+        s = specs[i]
+        P64 = np.asfortranarray(s.pumping, dtype=np.float64) if s.dim == 2 else np.asarray(s.pumping, np.float64)
+        u64 = np.asfortranarray(s.u0, dtype=np.complex128) if s.dim == 2 else np.asarray(s.u0, np.complex128)
+        flat = lambda a: np.ravel(a, order="K")
+        tu = T.tensor(flat(u64).copy(), device=dev)
+        tP = T.tensor(flat(P64).copy(), device=dev)
+        shp = (s.n, s.n) if s.dim == 2 else (s.n,)
+        tu = tu.reshape(shp)
+        tP = tP.reshape(shp)
+        T.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        ndev.solve_(tu, tP, order=s.order, dt=s.dt, dx=s.dx, coeffs=s.coeffs, iters=SOLVE_STEPS)
+        T.cuda.synchronize(dev)
+        plain_s += time.perf_counter() - t0
+        plain_ns += float(s.nodes) * SOLVE_STEPS
+        got = bs.get(k)
+        tg = T.tensor(np.ravel(got, order="K").copy(), device=dev).reshape(shp)
+        d, r = ndev.density_errors(tg, tu, tP, s.coeffs)
+        errs_d.append(d)
+        errs_n.append(r)
+    bs.close()
+    plain_rate = plain_ns / plain_s
+    result["plain_c128"] = {"value": plain_rate, "unit": UNIT,
+                            "sample": f"{len(sample_idx)} of the 512 instances, sequential complex128 solves, "
+                                      f"{SOLVE_STEPS} steps each (nls_solve_device)"}
+    result["batched_over_plain"] = value / ws / plain_rate
+    result["rel_l2_vs_c128"] = {"density_max": max(errs_d), "reservoir_max": max(errs_n),
+                                "sample": f"same {len(sample_idx)} instances after {SOLVE_STEPS} steps"}
+
+    # ---- end to end through the host-buffer C ABI: upload u0 and P, solve, download every state
+    h2d = sum(s.nodes * (8 + 4) for s in specs)
+    d2h = sum(s.nodes * 8 for s in specs)
+    e2e_times = []
+    for rep in range(max(1, min(args.steps, 2))):
+        ctx = b.ctx
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for i, s in enumerate(specs):
+            b.set(i, s.pumping, s.u0)
+        b.run(SOLVE_STEPS)
+        outs = [b.get(i) for i in range(len(specs))]
+        e2e_times.append(time.perf_counter() - t0)
+    e2e = float(total_nodes) * SOLVE_STEPS / float(np.mean(e2e_times))
+    result["e2e"] = {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                     "path": "nls_batch_set (host u0, P) -> nls_batch_run(5000) -> nls_batch_get (host u)"}
+    del outs
+
+    # ---- served stream (continuous batching) p50/p99
+    if args.serve > 0:
+        from nls_gb300.serve import Pool, serve
+        reqs = workloads.serve_stream(args.serve)
+        pool = Pool(dtype=np.complex64, budget_bytes=80 << 30, chunk_steps=500, device=local)
+        st = serve(reqs, rate=200.0, pool=pool)
+        pool.close()
+        result["serve"] = {"requests": args.serve, "rate_per_s": 200.0, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                           "node_steps_per_s": st["node_steps_per_s"], "wall_s": st["wall_s"],
+                           "budget_gb": 80, "chunk_steps": 500}
+
+    # ---- CPU oracle on the host cores (bounded sample)
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        samp = oracle_sample(specs)
+        rate, secs = cpu_oracle_rate(samp, 4, threads)
+        result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                  "sample": f"every 4th of the 512 instances ({len(samp)} solves) x 4 RK4 steps, "
+                                            f"float32 C++ restatement of nls/nls.f90, {secs:.1f} s"}
+    print(json.dumps(result))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--serve", type=int, default=400, help="requests in the served stream (0 = skip)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

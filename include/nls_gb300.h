@@ -1,0 +1,160 @@
+/* nls_gb300.h -- C ABI of the GB300 (sm_103a) solver for the nls time-stepping path.
+ *
+ * Drop-in boundary.  The reference exposes its native core as the f2py extension module
+ * `nls.native` with the Fortran module object `nls` (setup.py:69-79, nls/makefile:49, imported as
+ * `from .native import nls` in nls/solver.py:9).  Each entry point below names the reference
+ * routine it replaces.  Plain pointers and sizes only; every function returns an int status
+ * (NLS_OK = 0) and never aborts.  Host-buffer entry points follow the f2py call shape: inputs are
+ * read, a new result is written to the caller's buffer, nothing is retained between calls.
+ *
+ * Arrays: complex values are interleaved (re, im) pairs (complex128 for NLS_C128, complex64 for
+ * NLS_C64); real arrays (pump) are float64 or float32 to match.  2-D fields are n x n with the
+ * first Fortran index contiguous, exactly the memory of the reference's Fortran (n, n) arrays.
+ * The 23-slot coefficient vector is always float64 and indexed like the reference's coeffs(1..23)
+ * shifted to 0-based.
+ */
+#ifndef NLS_GB300_H
+#define NLS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------ */
+#define NLS_OK 0
+#define NLS_ERR_INVALID 1     /* bad argument: size, pointer, coefficient vector, dtype */
+#define NLS_ERR_ORDER 2       /* unsupported stencil order (1-D: 3, 5, 7; 2-D: 3, 5) */
+#define NLS_ERR_CUDA 3        /* CUDA runtime error; nls_last_error() has the text */
+#define NLS_ERR_NONFINITE 4   /* NaN or Inf found in a result by the FP64 diagnostics */
+#define NLS_ERR_TIMEOUT 5     /* a bounded wait expired */
+#define NLS_ERR_NOMEM 6       /* device memory exhausted */
+#define NLS_ERR_BUSY 7        /* serving pool: no slot or admission budget for this request now */
+#define NLS_ERR_NOT_READY 8   /* serving pool: nothing finished yet */
+
+/* ---- precisions -------------------------------------------------------------------------- */
+#define NLS_C128 0            /* complex128 state, float64 pump: the plain (drop-in) path */
+#define NLS_C64 1             /* complex64 state, float32 pump: the precision form */
+
+typedef struct nls_ctx nls_ctx;
+typedef struct nls_batch nls_batch;
+typedef struct nls_pool nls_pool;
+
+/* One solve: dim 1 is the radial 1-D model of solve_nls (nls/nls.f90:797-813), dim 2 the
+ * Cartesian model of solve_nls_2d (nls/nls.f90:903-919).  variant selects a kernel shape chosen by
+ * the autotuner (-1 = built-in choice): 1-D = CTAs per solve (cluster size 1..16, 0 = unfused
+ * stage kernels); 2-D = 0 unfused, 1 tile 64x64, 2 tile 128x32, 3 tile 32x32. */
+typedef struct nls_problem {
+  int dim;
+  int n;
+  int order;
+  int variant;
+  double dt;
+  double dx;
+  double coeffs[23];
+} nls_problem;
+
+/* version(major, minor, patch) -- nls/nls.f90:29-37 (reports the reference's 0.2.0). */
+int nls_version(int* major, int* minor, int* patch);
+
+/* make_laplacian(n, m, h, op) -- nls/nls.f90:278-295.  op: (order, n) column-major band storage,
+ * float64.  Host only; needs no GPU. */
+int nls_make_laplacian(int n, int order, double h, double* op);
+
+/* make_laplacian_2d(n, m, h, blocks, orders) -- nls/nls.f90:388-403 (orders 3 and 5; the
+ * reference's order-7 block array is mis-dimensioned, nls/nls.f90:360).  blocks: (n, 2*order-1)
+ * column-major float64; orders: int[order].  Host only. */
+int nls_make_laplacian_2d(int n, int order, double h, double* blocks, int* orders);
+
+/* ---- context ----------------------------------------------------------------------------- */
+int nls_ctx_create(int device, nls_ctx** out);
+int nls_ctx_destroy(nls_ctx* ctx);
+/* The context's own (non-blocking) cudaStream_t: every launch and copy of this context is
+ * ordered on it, so callers record events on it and order their own work after it. */
+int nls_ctx_stream(nls_ctx* ctx, void** stream);
+int nls_ctx_synchronize(nls_ctx* ctx);
+/* Text of the last failure on this context (empty string if none); valid until the next call. */
+const char* nls_last_error(nls_ctx* ctx);
+/* Number of kernel launches this context has issued (graph replays count every node). */
+int64_t nls_ctx_launch_count(nls_ctx* ctx);
+
+/* ---- single solves ----------------------------------------------------------------------- */
+/* u = solve_nls(dt, dx, order, iters, pumping, coeffs, u0, [n]) -- nls/nls.f90:797-813, also
+ * solve_nls_1d (:815-827).  Host buffers; blocks until u is written. */
+int nls_solve_1d(nls_ctx* ctx, int dtype, double dt, double dx, int n, int order, int iters,
+                 const double* coeffs23, const void* pumping, const void* u0, void* u);
+
+/* u = solve_nls_2d(dt, dx, order, iters, pumping, coeffs, u0, [n]) -- nls/nls.f90:903-919. */
+int nls_solve_2d(nls_ctx* ctx, int dtype, double dt, double dx, int n, int order, int iters,
+                 const double* coeffs23, const void* pumping, const void* u0, void* u);
+
+/* Device-resident form of both: advances the state u_dev in place by iters RK4 steps on the
+ * context's stream (no host synchronisation).  pumping_dev and u_dev are device pointers.
+ * Replaces the same routines; used for resume (repeated solve(k) from the last state). */
+int nls_solve_device(nls_ctx* ctx, int dtype, const nls_problem* problem, int64_t iters,
+                     const void* pumping_dev, void* u_dev);
+
+/* mu = chemical_potential_1d(dx, pumping, coeffs, u0, [n]) -- nls/nls.f90:921-948 (complex). */
+int nls_chemical_potential_1d(nls_ctx* ctx, int dtype, double dx, int n, const double* coeffs23,
+                              const void* pumping, const void* u0, double* mu_re, double* mu_im);
+
+/* mu = chemical_potential_2d(dx, pumping, coeffs, u0, [n]) -- nls/nls.f90:950-971 (real part). */
+int nls_chemical_potential_2d(nls_ctx* ctx, int dtype, double dx, int n, const double* coeffs23,
+                              const void* pumping, const void* u0, double* mu);
+
+/* ---- FP64 device diagnostics (no reference counterpart: the reference has none) ----------- */
+/* sum |u|^2 over count nodes and the number of non-finite components; blocks until done. */
+int nls_norm_device(nls_ctx* ctx, int dtype, int64_t count, const void* u_dev, double* sum_sq,
+                    int64_t* nonfinite);
+/* Relative L2 errors of the density |u|^2 and of the reservoir n = c12 P / (c13 + c14 |u|^2)
+ * (nls/model.py:376-380) of u_dev against a complex128 reference state; pumping_f64_dev is the
+ * float64 pump.  Blocks until done. */
+int nls_density_error_device(nls_ctx* ctx, int dtype, int64_t count, const void* u_dev,
+                             const void* u_ref_c128_dev, const double* pumping_f64_dev, double c12,
+                             double c13, double c14, double* rel_l2_density,
+                             double* rel_l2_reservoir);
+
+/* ---- batched form: many independent solves, one graph-captured launch sequence ------------ */
+/* Replaces running Model.solve() once per configuration (the reference's benchmark and job farm,
+ * benchmark/benchmark.py:21-76, schedulr/workr.py:39-66) with one resident batch on the GPU. */
+int nls_batch_create(nls_ctx* ctx, int dtype, int count, const nls_problem* problems,
+                     nls_batch** out);
+/* Upload instance index's pump and initial state from host buffers (sizes from its problem). */
+int nls_batch_set(nls_batch* batch, int index, const void* pumping, const void* u0);
+/* Advance every instance by steps RK4 steps (a CUDA graph, replayed from cache). Asynchronous. */
+int nls_batch_run(nls_batch* batch, int64_t steps);
+/* Copy instance index's current state to a host buffer; blocks until written. */
+int nls_batch_get(nls_batch* batch, int index, void* u);
+/* Device pointers of instance index's current state and pump (valid until the next run). */
+int nls_batch_state(nls_batch* batch, int index, void** u_dev, const void** pumping_dev);
+/* Kernel launches one run(steps) issues, and nodes summed over instances. */
+int nls_batch_info(nls_batch* batch, int64_t steps, int64_t* launches, int64_t* total_nodes);
+int nls_batch_destroy(nls_batch* batch);
+
+/* ---- serving pool: continuous batching under an HBM budget -------------------------------- */
+/* Replaces schedulr's pull queue of independent solves (schedulr/schedulr.py:48-154,
+ * schedulr/workr.py:88-102) with in-process admission into a resident, continuously batched
+ * set of solves.  budget_bytes bounds the device memory of admitted states and pumps. */
+int nls_pool_create(nls_ctx* ctx, int dtype, size_t budget_bytes, int max_slots, int chunk_steps,
+                    nls_pool** out);
+/* Admit one request (host buffers are copied before return).  NLS_ERR_BUSY if no slot or budget
+ * is free now; the caller keeps it queued and retries after nls_pool_step. */
+int nls_pool_admit(nls_pool* pool, const nls_problem* problem, const void* pumping,
+                   const void* u0, int64_t steps, int64_t tag, int* slot);
+/* Advance every admitted request by up to chunk_steps RK4 steps (each stops at its own count).
+ * Blocks until the chunk is done; *finished = requests that completed in this chunk. */
+int nls_pool_step(nls_pool* pool, int* finished);
+/* Take one finished request: its tag and final state (host buffer of its size); frees its slot
+ * and budget.  NLS_ERR_NOT_READY if none is finished. */
+int nls_pool_take(nls_pool* pool, int64_t* tag, void* u, size_t u_bytes);
+/* Admitted-but-unfinished requests, bytes of budget in use. */
+int nls_pool_status(nls_pool* pool, int* active, size_t* bytes_in_use);
+int nls_pool_destroy(nls_pool* pool);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NLS_GB300_H */

@@ -1,0 +1,386 @@
+// k1d.cu -- 1-D (axially symmetric, radial) RK4 kernels for sm_103a.
+//
+// rk4_1d_resident: the whole grid of one solve lives in shared memory of one CTA or of a thread
+// block cluster (distributed shared memory) for every step of the launch.  Each RK4 stage
+// (nls/nls.f90:726-729) reads the previous stage's values from shared memory, evaluates the
+// radial Laplacian (make_laplacian, nls/nls.f90:132-295) and the pointwise terms of
+// `hamiltonian` (nls/nls.f90:621-650), and writes the next stage input; CTAs of a cluster push
+// their K edge values into their neighbours' halo slots and meet at one cluster barrier per
+// stage.  HBM is touched once per launch (load and store of the state).
+//
+// rk4_1d_stage: one RK4 stage over an arbitrary-size grid from global memory, the general path
+// for grids too large to stay resident.
+#include <cooperative_groups.h>
+
+#include "kernels.h"
+#include "nls_common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace nlsg {
+
+template <typename T, int K>
+struct Weights1D {
+  T w2[2 * K + 1];
+  T w1[2 * K + 1];
+};
+
+template <typename T, int K>
+__device__ __forceinline__ Weights1D<T, K> load_w(const Stencil1D& s) {
+  Weights1D<T, K> w;
+#pragma unroll
+  for (int i = 0; i < 2 * K + 1; ++i) {
+    w.w2[i] = (T)s.w2[i];
+    w.w1[i] = (T)s.w1[i];
+  }
+  return w;
+}
+
+// (L u)_p from a buffer whose element c holds u_p (and c +- d hold u_{p +- d}).
+template <typename T, int K>
+__device__ __forceinline__ typename C2<T>::type lap1d(const typename C2<T>::type* in, int c, int p,
+                                                      T inv_r, const Weights1D<T, K>& w,
+                                                      const Stencil1D& s) {
+  typedef typename C2<T>::type C;
+  C lu;
+  if (p >= K) {
+    T d2x = 0, d2y = 0, d1x = 0, d1y = 0;
+#pragma unroll
+    for (int d = -K; d <= K; ++d) {
+      C v = in[c + d];
+      d2x += w.w2[d + K] * v.x;
+      d2y += w.w2[d + K] * v.y;
+      if (d != 0) {
+        d1x += w.w1[d + K] * v.x;
+        d1y += w.w1[d + K] * v.y;
+      }
+    }
+    lu.x = d2x + inv_r * d1x;
+    lu.y = d2y + inv_r * d1y;
+  } else {
+    T lx = 0, ly = 0;
+#pragma unroll
+    for (int d = -K; d <= K; ++d) {
+      T a = (T)s.near[p][d + K];
+      C v = in[c + d];
+      lx += a * v.x;
+      ly += a * v.y;
+    }
+    lu.x = lx;
+    lu.y = ly;
+  }
+  return lu;
+}
+
+template <typename T, int K, int NPT>
+__global__ void __launch_bounds__(512) rk4_1d_resident(const Inst1D* __restrict__ insts, int cl,
+                                                       int seg_cap) {
+  typedef typename C2<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int inst = blockIdx.x / cl;
+  const int rank = blockIdx.x % cl;
+  const Inst1D& I = insts[inst];
+  const int n = I.n;
+  const int seg = (n + cl - 1) / cl;
+  const int p0 = rank * seg;
+  const int len = max(0, min(seg, n - p0));
+  const int NT = blockDim.x;
+  const int tid = threadIdx.x;
+  const int L = seg_cap + 2 * K;
+  C* buf[2] = {reinterpret_cast<C*>(smem_raw), reinterpret_cast<C*>(smem_raw) + L};
+
+  cg::cluster_group cluster = cg::this_cluster();
+  C* left_buf[2] = {nullptr, nullptr};
+  C* right_buf[2] = {nullptr, nullptr};
+  if (cl > 1) {
+    if (rank > 0) {
+      left_buf[0] = cluster.map_shared_rank(buf[0], rank - 1);
+      left_buf[1] = cluster.map_shared_rank(buf[1], rank - 1);
+    }
+    if (rank < cl - 1) {
+      right_buf[0] = cluster.map_shared_rank(buf[0], rank + 1);
+      right_buf[1] = cluster.map_shared_rank(buf[1], rank + 1);
+    }
+  }
+
+  for (int i = tid; i < 2 * L; i += NT) buf[0][i] = mk<T>(0, 0);
+  if (cl > 1) cluster.sync(); else __syncthreads();
+
+  const Phys<T> ph = phys_from<T>(I.ph);
+  const RK<T> rk = rk_from<T>(I.dt);
+  const Weights1D<T, K> w = load_w<T, K>(I.op);
+  const T h = (T)I.op.h;
+  const C* __restrict__ Ug = reinterpret_cast<const C*>(I.u);
+  const T* __restrict__ Pg = reinterpret_cast<const T*>(I.P);
+
+  C u[NPT], acc[NPT];
+  T P[NPT], ir[NPT];
+#pragma unroll
+  for (int j = 0; j < NPT; ++j) {
+    const int li = tid + j * NT;
+    u[j] = mk<T>(0, 0);
+    acc[j] = mk<T>(0, 0);
+    P[j] = 0;
+    ir[j] = 0;
+    if (li < len) {
+      const int p = p0 + li;
+      u[j] = Ug[p];
+      P[j] = Pg[p];
+      ir[j] = p >= K ? (T)1 / ((T)p * h) : (T)0;
+      buf[0][K + li] = u[j];
+      if (left_buf[0] && li < K) left_buf[0][seg + K + li] = u[j];
+      if (right_buf[0] && li >= seg - K) right_buf[0][li - (seg - K)] = u[j];
+    }
+  }
+  if (cl > 1) cluster.sync(); else __syncthreads();
+
+  const int64_t steps = I.steps;
+  for (int64_t step = 0; step < steps; ++step) {
+#pragma unroll 1
+    for (int s = 1; s <= 4; ++s) {
+      const C* in = buf[(s & 1) ? 0 : 1];
+      const int ob = (s & 1) ? 1 : 0;
+      C* out = buf[ob];
+#pragma unroll
+      for (int j = 0; j < NPT; ++j) {
+        const int li = tid + j * NT;
+        if (li < len) {
+          const int p = p0 + li;
+          const int c = K + li;
+          const C lu = lap1d<T, K>(in, c, p, ir[j], w, I.op);
+          const C k = rhs<T>(in[c], P[j], lu, ph);
+          C t;
+          if (s == 1) {
+            acc[j] = k;
+            t.x = u[j].x + rk.half_dt * k.x;
+            t.y = u[j].y + rk.half_dt * k.y;
+          } else if (s == 2) {
+            acc[j].x += (T)2 * k.x;
+            acc[j].y += (T)2 * k.y;
+            t.x = u[j].x + rk.half_dt * k.x;
+            t.y = u[j].y + rk.half_dt * k.y;
+          } else if (s == 3) {
+            acc[j].x += (T)2 * k.x;
+            acc[j].y += (T)2 * k.y;
+            t.x = u[j].x + rk.dt * k.x;
+            t.y = u[j].y + rk.dt * k.y;
+          } else {
+            acc[j].x += k.x;
+            acc[j].y += k.y;
+            u[j].x = u[j].x + rk.dt6 * acc[j].x;
+            u[j].y = u[j].y + rk.dt6 * acc[j].y;
+            t = u[j];
+          }
+          out[c] = t;
+          if (left_buf[ob] && li < K) left_buf[ob][seg + K + li] = t;
+          if (right_buf[ob] && li >= seg - K) right_buf[ob][li - (seg - K)] = t;
+        }
+      }
+      if (cl > 1) cluster.sync(); else __syncthreads();
+    }
+  }
+
+  C* __restrict__ Uo = reinterpret_cast<C*>(I.u);
+#pragma unroll
+  for (int j = 0; j < NPT; ++j) {
+    const int li = tid + j * NT;
+    if (li < len) Uo[p0 + li] = u[j];
+  }
+  if (cl > 1) cluster.sync();
+}
+
+// One RK4 stage of a 1-D grid held in global memory (see nls_common.cuh for the stage scheme).
+template <typename T, int K>
+__global__ void __launch_bounds__(256) rk4_1d_stage(int n, int s, const void* __restrict__ src_,
+                                                    void* __restrict__ u_, const void* __restrict__ P_,
+                                                    void* __restrict__ acc_, void* __restrict__ dst_,
+                                                    double dt, PhysD phd, Stencil1D op) {
+  typedef typename C2<T>::type C;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const C* __restrict__ src = reinterpret_cast<const C*>(src_);
+  C* __restrict__ U = reinterpret_cast<C*>(u_);
+  const T* __restrict__ P = reinterpret_cast<const T*>(P_);
+  C* __restrict__ acc = reinterpret_cast<C*>(acc_);
+  C* __restrict__ dst = reinterpret_cast<C*>(dst_);
+  const Phys<T> ph = phys_from<T>(phd);
+  const RK<T> rk = rk_from<T>(dt);
+  const Weights1D<T, K> w = load_w<T, K>(op);
+  // gather the 2K+1 neighbours with zero outside [0, n)
+  C v[2 * K + 1];
+#pragma unroll
+  for (int d = -K; d <= K; ++d) {
+    const int q = p + d;
+    v[d + K] = (q >= 0 && q < n) ? src[q] : mk<T>(0, 0);
+  }
+  const T ir = p >= K ? (T)1 / ((T)p * (T)op.h) : (T)0;
+  const C lu = lap1d<T, K>(v, K, p, ir, w, op);
+  const C k = rhs<T>(v[K], P[p], lu, ph);
+  const C u = U[p];
+  if (s == 1) {
+    acc[p] = k;
+    dst[p] = mk<T>(u.x + rk.half_dt * k.x, u.y + rk.half_dt * k.y);
+  } else if (s == 2 || s == 3) {
+    C a = acc[p];
+    a.x += (T)2 * k.x;
+    a.y += (T)2 * k.y;
+    acc[p] = a;
+    const T c = s == 2 ? rk.half_dt : rk.dt;
+    dst[p] = mk<T>(u.x + c * k.x, u.y + c * k.y);
+  } else {
+    C a = acc[p];
+    a.x += k.x;
+    a.y += k.y;
+    U[p] = mk<T>(u.x + rk.dt6 * a.x, u.y + rk.dt6 * a.y);
+  }
+}
+
+// v = H(u) for the diagnostics (chemical potential).
+template <typename T, int K>
+__global__ void __launch_bounds__(256) rhs_1d(int n, const void* __restrict__ u_, const void* __restrict__ P_,
+                                              void* __restrict__ v_, PhysD phd, Stencil1D op) {
+  typedef typename C2<T>::type C;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const C* __restrict__ u = reinterpret_cast<const C*>(u_);
+  const T* __restrict__ P = reinterpret_cast<const T*>(P_);
+  const Phys<T> ph = phys_from<T>(phd);
+  const Weights1D<T, K> w = load_w<T, K>(op);
+  C v[2 * K + 1];
+#pragma unroll
+  for (int d = -K; d <= K; ++d) {
+    const int q = p + d;
+    v[d + K] = (q >= 0 && q < n) ? u[q] : mk<T>(0, 0);
+  }
+  const T ir = p >= K ? (T)1 / ((T)p * (T)op.h) : (T)0;
+  reinterpret_cast<C*>(v_)[p] = rhs<T>(v[K], P[p], lap1d<T, K>(v, K, p, ir, w, op), ph);
+}
+
+// ------------------------------------------------------------------ launchers
+
+template <typename T, int K, int NPT>
+static cudaError_t launch_res(const Inst1D* d_insts, int count, int cl, int seg_cap, int nt,
+                              cudaStream_t stream, bool prepare_only) {
+  auto kern = rk4_1d_resident<T, K, NPT>;
+  const size_t smem = (size_t)2 * (seg_cap + 2 * K) * sizeof(typename C2<T>::type);
+  // Attributes are raised once, monotonically, so launches inside a stream capture never need
+  // to change them (prepare_1d_resident runs before any capture).
+  static size_t configured_smem = 0;
+  static bool non_portable = false;
+  if (smem > configured_smem) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured_smem = smem;
+  }
+  if (cl > 8 && !non_portable) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    non_portable = true;
+  }
+  if (prepare_only) return cudaSuccess;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(count * cl);
+  cfg.blockDim = dim3(nt);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, d_insts, cl, seg_cap);
+}
+
+template <typename T, int K>
+static cudaError_t launch_res_npt(const Inst1D* d, int count, int cl, int seg_cap, cudaStream_t s,
+                                  bool prepare_only) {
+  // threads: up to 512; nodes per thread: 1, 2, 4 or 8 (8 only in single precision)
+  int npt = 1;
+  while (npt * 512 < seg_cap) npt *= 2;
+  int nt = (seg_cap + npt - 1) / npt;
+  nt = ((nt + 31) / 32) * 32;
+  if (nt > 512) nt = 512;
+  switch (npt) {
+    case 1: return launch_res<T, K, 1>(d, count, cl, seg_cap, nt, s, prepare_only);
+    case 2: return launch_res<T, K, 2>(d, count, cl, seg_cap, nt, s, prepare_only);
+    case 4: return launch_res<T, K, 4>(d, count, cl, seg_cap, nt, s, prepare_only);
+    case 8:
+      if (sizeof(T) == 4) return launch_res<T, K, 8>(d, count, cl, seg_cap, nt, s, prepare_only);
+      return cudaErrorInvalidValue;
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+static cudaError_t dispatch_res(int dtype, int K, const Inst1D* d_insts, int count, int cl,
+                                int seg_cap, cudaStream_t s, bool prepare_only) {
+  if (dtype == NLS_C128) {
+    if (K == 1) return launch_res_npt<double, 1>(d_insts, count, cl, seg_cap, s, prepare_only);
+    if (K == 2) return launch_res_npt<double, 2>(d_insts, count, cl, seg_cap, s, prepare_only);
+    if (K == 3) return launch_res_npt<double, 3>(d_insts, count, cl, seg_cap, s, prepare_only);
+  } else {
+    if (K == 1) return launch_res_npt<float, 1>(d_insts, count, cl, seg_cap, s, prepare_only);
+    if (K == 2) return launch_res_npt<float, 2>(d_insts, count, cl, seg_cap, s, prepare_only);
+    if (K == 3) return launch_res_npt<float, 3>(d_insts, count, cl, seg_cap, s, prepare_only);
+  }
+  return cudaErrorInvalidValue;
+}
+
+int resident_1d_seg_limit(int dtype) { return dtype == NLS_C128 ? 2048 : 4096; }
+
+cudaError_t prepare_1d_resident(int dtype, int K, int cl, int seg_cap) {
+  if (seg_cap > resident_1d_seg_limit(dtype) || cl < 1 || cl > 16) return cudaErrorInvalidValue;
+  return dispatch_res(dtype, K, nullptr, 0, cl, seg_cap, nullptr, true);
+}
+
+cudaError_t launch_1d_resident(int dtype, int K, const Inst1D* d_insts, int count, int cl,
+                               int seg_cap, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  if (seg_cap > resident_1d_seg_limit(dtype) || cl < 1 || cl > 16) return cudaErrorInvalidValue;
+  return dispatch_res(dtype, K, d_insts, count, cl, seg_cap, s, false);
+}
+
+template <typename T, int K>
+static void stage_1d_t(int n, int s, const void* src, void* u, const void* P, void* acc, void* dst,
+                       double dt, const PhysD& ph, const Stencil1D& op, cudaStream_t st) {
+  rk4_1d_stage<T, K><<<(n + 255) / 256, 256, 0, st>>>(n, s, src, u, P, acc, dst, dt, ph, op);
+}
+
+cudaError_t launch_1d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,
+                            void* acc, void* dst, double dt, const PhysD& ph, const Stencil1D& op,
+                            cudaStream_t st) {
+  const int K = op.K;
+  if (dtype == NLS_C128) {
+    if (K == 1) stage_1d_t<double, 1>(n, s, src, u, P, acc, dst, dt, ph, op, st);
+    else if (K == 2) stage_1d_t<double, 2>(n, s, src, u, P, acc, dst, dt, ph, op, st);
+    else if (K == 3) stage_1d_t<double, 3>(n, s, src, u, P, acc, dst, dt, ph, op, st);
+    else return cudaErrorInvalidValue;
+  } else {
+    if (K == 1) stage_1d_t<float, 1>(n, s, src, u, P, acc, dst, dt, ph, op, st);
+    else if (K == 2) stage_1d_t<float, 2>(n, s, src, u, P, acc, dst, dt, ph, op, st);
+    else if (K == 3) stage_1d_t<float, 3>(n, s, src, u, P, acc, dst, dt, ph, op, st);
+    else return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rhs_1d(int dtype, int n, const void* u, const void* P, void* v, const PhysD& ph,
+                          const Stencil1D& op, cudaStream_t st) {
+  const int K = op.K;
+  const int g = (n + 255) / 256;
+  if (dtype == NLS_C128) {
+    if (K == 1) rhs_1d<double, 1><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
+    else if (K == 2) rhs_1d<double, 2><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
+    else if (K == 3) rhs_1d<double, 3><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
+    else return cudaErrorInvalidValue;
+  } else {
+    if (K == 1) rhs_1d<float, 1><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
+    else if (K == 2) rhs_1d<float, 2><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
+    else if (K == 3) rhs_1d<float, 3><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
+    else return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace nlsg

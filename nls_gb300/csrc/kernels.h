@@ -1,0 +1,68 @@
+// kernels.h -- host-side launchers of the sm_103a kernels (internal to libnls_gb300).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "nls_types.h"
+
+// dtype codes shared with the public C ABI
+#ifndef NLS_C128
+#define NLS_C128 0
+#define NLS_C64 1
+#endif
+
+namespace nlsg {
+
+// ---- 1-D
+int resident_1d_seg_limit(int dtype);
+// Sets the kernel attributes a later launch with these parameters needs (call outside capture).
+cudaError_t prepare_1d_resident(int dtype, int K, int cl, int seg_cap);
+cudaError_t launch_1d_resident(int dtype, int K, const Inst1D* d_insts, int count, int cl,
+                               int seg_cap, cudaStream_t s);
+cudaError_t launch_1d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,
+                            void* acc, void* dst, double dt, const PhysD& ph, const Stencil1D& op,
+                            cudaStream_t st);
+cudaError_t launch_rhs_1d(int dtype, int n, const void* u, const void* P, void* v, const PhysD& ph,
+                          const Stencil1D& op, cudaStream_t st);
+
+// ---- 2-D
+// Fused-step tile shapes (region = tile + halo of 4K on every side).
+enum TileShape2D {
+  TILE_UNFUSED = 0,   // four stage launches per step, no halo recomputation
+  TILE_64x64 = 1,     // region 64 x 64, 256 threads (single precision)
+  TILE_128x32 = 2,    // region 128 x 32, 256 threads (single precision)
+  TILE_32x32 = 3,     // region 32 x 32, 256 threads (either precision)
+};
+int tile_region_x(int shape);
+int tile_region_y(int shape);
+int tile_out_x(int shape, int K);
+int tile_out_y(int shape, int K);
+bool tile_supported(int shape, int dtype);
+// CTAs per SM the fused kernel reaches (for persistent grid sizing)
+int fused_2d_blocks_per_sm(int dtype, int K, int shape);
+cudaError_t launch_2d_fused(int dtype, int K, int shape, const Inst2D* d_insts,
+                            const TileItem* d_items, int n_items, int j_step, int grid,
+                            cudaStream_t s);
+cudaError_t launch_2d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,
+                            void* acc, void* dst, double dt, const PhysD& ph, const Stencil2D& op,
+                            cudaStream_t st);
+cudaError_t launch_rhs_2d(int dtype, int n, const void* u, const void* P, void* v, const PhysD& ph,
+                          const Stencil2D& op, cudaStream_t st);
+
+// ---- diagnostics (FP64 accumulation, deterministic two-pass reductions)
+// Sums over n nodes, written to out[0..]:
+//   norm:   out[0] = sum w_i |u_i|^2, out[1] = number of non-finite components
+//   mu:     out[0..3] = sum w conj(u) v (re, im), sum w |u|^2 (re), 0
+//   relerr: out[0] = sum (|a|^2 - |b|^2)^2, out[1] = sum |b|^4,
+//           out[2] = sum (n_a - n_b)^2,     out[3] = sum n_b^2,  n = c12 P / (c13 + c14 |.|^2)
+// weight mode: 0 = 1, 1 = radial r_i = i * dx (1-D chemical potential, nls/nls.f90:941-946)
+size_t diag_partials_bytes(long long n);
+cudaError_t diag_norm(int dtype, long long n, const void* u, int weight_mode, double dx,
+                      double* d_partials, double* d_out, cudaStream_t st);
+cudaError_t diag_mu(int dtype, long long n, const void* u, const void* v, int weight_mode,
+                    double dx, double* d_partials, double* d_out, cudaStream_t st);
+cudaError_t diag_relerr(int dtype_a, long long n, const void* a, const void* b_c128,
+                        const double* P, double c12, double c13, double c14, double* d_partials,
+                        double* d_out, cudaStream_t st);
+
+}  // namespace nlsg

@@ -1,0 +1,108 @@
+"""Device-resident solves on torch CUDA tensors (resume without re-upload).
+
+The reference resumes a run by ``model.setInitialSolution(prev)`` followed by ``solve(k)``
+(nls/animation.py:65-66, tools/check.py:35-36), which re-sends the state through f2py each time.
+Here the state stays on the GPU: ``solve_(u, P, ...)`` advances the complex tensor ``u`` in place.
+Work runs on the library context's stream; the calls order themselves after torch's current
+stream and make it wait for the result, so ordinary torch code can use ``u`` right after.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def _ext_stream(ctx: _lib.Context) -> torch.cuda.ExternalStream:
+    s = getattr(ctx, "_torch_stream", None)
+    if s is None:
+        s = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", ctx.device))
+        ctx._torch_stream = s
+    return s
+
+
+def context(device: int = 0) -> _lib.Context:
+    return _lib.default_context(device)
+
+
+def stream(device: int = 0) -> torch.cuda.ExternalStream:
+    """The torch view of the stream every kernel of this library is launched on."""
+    return _ext_stream(context(device))
+
+
+def _code_of(u: torch.Tensor) -> int:
+    if u.dtype == torch.complex128:
+        return _lib.NLS_C128
+    if u.dtype == torch.complex64:
+        return _lib.NLS_C64
+    raise TypeError("state must be complex64 or complex128")
+
+
+def solve_(u: torch.Tensor, P: torch.Tensor, *, order: int, dt: float, dx: float, coeffs, iters: int,
+           variant: int = -1) -> torch.Tensor:
+    """Advance u (shape (n,) for the radial model or (n, n) for the 2-D model) by iters RK4 steps.
+
+    For 2-D, memory order follows the reference's Fortran arrays: the last torch dimension is
+    the contiguous one and plays the role of the Fortran first index (the cross stencils are
+    symmetric, so this only fixes the order of floating-point operations)."""
+    if not u.is_cuda or not P.is_cuda:
+        raise ValueError("u and P must be CUDA tensors")
+    if not u.is_contiguous() or not P.is_contiguous():
+        raise ValueError("u and P must be contiguous")
+    code = _code_of(u)
+    want_p = torch.float64 if code == _lib.NLS_C128 else torch.float32
+    if P.dtype != want_p or P.shape != u.shape:
+        raise ValueError(f"P must be {want_p} with the shape of u")
+    dim = u.dim()
+    if dim not in (1, 2) or (dim == 2 and u.shape[0] != u.shape[1]):
+        raise ValueError("u must be (n,) or (n, n)")
+    ctx = context(u.device.index or 0)
+    pr = _lib.make_problem(dim, u.shape[0], order, dt, dx, coeffs, variant)
+    ext = _ext_stream(ctx)
+    ext.wait_stream(torch.cuda.current_stream(u.device))
+    st = _lib.lib().nls_solve_device(ctx.handle, code, ctypes.byref(pr), int(iters),
+                                     ctypes.c_void_p(P.data_ptr()), ctypes.c_void_p(u.data_ptr()))
+    _lib.check(st, "nls_solve_device", ctx.handle)
+    torch.cuda.current_stream(u.device).wait_stream(ext)
+    u.record_stream(ext)
+    P.record_stream(ext)
+    return u
+
+
+def norm(u: torch.Tensor) -> float:
+    """FP64 sum of |u|^2 over all nodes; raises if any component is non-finite."""
+    ctx = context(u.device.index or 0)
+    ext = _ext_stream(ctx)
+    ext.wait_stream(torch.cuda.current_stream(u.device))
+    s = ctypes.c_double()
+    bad = ctypes.c_int64()
+    st = _lib.lib().nls_norm_device(ctx.handle, _code_of(u), u.numel(), ctypes.c_void_p(u.data_ptr()),
+                                    ctypes.byref(s), ctypes.byref(bad))
+    _lib.check(st, "nls_norm_device", ctx.handle)
+    return s.value
+
+
+def density_errors(u: torch.Tensor, u_ref: torch.Tensor, P64: torch.Tensor, coeffs):
+    """Relative L2 errors of |u|^2 and of the reservoir n against a complex128 reference."""
+    if u_ref.dtype != torch.complex128 or P64.dtype != torch.float64:
+        raise ValueError("reference must be complex128 with a float64 pump")
+    c = np.asarray(coeffs, dtype=np.float64)
+    ctx = context(u.device.index or 0)
+    ext = _ext_stream(ctx)
+    ext.wait_stream(torch.cuda.current_stream(u.device))
+    d, r = ctypes.c_double(), ctypes.c_double()
+    st = _lib.lib().nls_density_error_device(ctx.handle, _code_of(u), u.numel(), ctypes.c_void_p(u.data_ptr()),
+                                             ctypes.c_void_p(u_ref.data_ptr()), ctypes.c_void_p(P64.data_ptr()),
+                                             float(c[11]), float(c[12]), float(c[13]), ctypes.byref(d),
+                                             ctypes.byref(r))
+    _lib.check(st, "nls_density_error_device", ctx.handle)
+    return d.value, r.value
+
+
+def launches(device: int = 0) -> int:
+    """Kernel launches issued so far by this process's context on the device."""
+    return context(device).launches

@@ -1,0 +1,306 @@
+"""GPU parity: every kernel path of libnls_gb300.so against the CPU oracle.
+
+Tolerances (relative L2 over the whole field):
+* complex128 path vs the float64 oracle: <= 1e-10 (the drop-in contract);
+* complex64 form vs the float32 oracle: <= 3e-5; vs the float64 oracle on |psi|^2 and on the
+  reservoir n: <= 1e-4 (the precision form's contract);
+* batched, served and resumed results vs single solves on the same kernel path: bit-identical.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import torch
+    from nls_gb300 import build
+    build.build()
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    from nls_gb300 import _lib
+    _lib.lib()
+    return torch
+
+
+def _spec_1d(n, order, seed=0, dt=1e-4, dx=0.04):
+    from nls_gb300 import workloads as w
+    s, _ = w.plain_1d(n=n, length=n * dx, order=order, dt=dt, seed=seed)
+    return s
+
+
+def _spec_2d(n, order, seed=0, dt=5e-5, dx=0.15625):
+    from nls_gb300 import workloads as w
+    s, _ = w.plain_2d(n=n, length=n * dx, order=order, dt=dt, seed=seed)
+    return s
+
+
+def _device_solve(torch, s, iters, dtype, variant):
+    from nls_gb300 import device
+    ct = torch.complex128 if dtype == np.complex128 else torch.complex64
+    rt = torch.float64 if dtype == np.complex128 else torch.float32
+    # 2-D: torch row-major (n, n) with the last index contiguous == Fortran-order numpy memory
+    u0 = np.asarray(s.u0).T if s.dim == 2 else s.u0
+    P = np.asarray(s.pumping).T if s.dim == 2 else s.pumping
+    u = torch.tensor(np.ascontiguousarray(u0), dtype=ct, device="cuda")
+    Pt = torch.tensor(np.ascontiguousarray(P), dtype=rt, device="cuda")
+    device.solve_(u, Pt, order=s.order, dt=s.dt, dx=s.dx, coeffs=s.coeffs, iters=iters, variant=variant)
+    out = u.cpu().numpy()
+    return out.T if s.dim == 2 else out
+
+
+# ------------------------------------------------------------------ complex128 drop-in path
+
+@pytest.mark.parametrize("order", [3, 5, 7])
+@pytest.mark.parametrize("variant", [-1, 1, 2, 4, 16, 0])
+def test_1d_c128_matches_oracle(gpu, oracle_lib, order, variant):
+    s = _spec_1d(257, order)
+    iters = 300
+    want = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float64)
+    got = _device_solve(gpu, s, iters, np.complex128, variant)
+    assert rel(got, want) <= 1e-10
+
+
+def test_1d_plain_config_full(gpu, oracle_lib):
+    """1000 nodes on [0, 40], order 5, dt 1e-4, 10 000 steps, through the f2py-shaped API."""
+    from nls_gb300 import workloads as w
+    from nls_gb300.native import nls
+    s, steps = w.plain_1d()
+    want = oracle_lib.solve(s.dt, s.dx, s.order, steps, s.pumping, s.coeffs, s.u0, dtype=np.float64)
+    got = nls.solve_nls(s.dt, s.dx, s.order, steps, s.pumping, s.coeffs, s.u0)
+    assert got.dtype == np.complex128
+    assert rel(got, want) <= 1e-10
+
+
+@pytest.mark.parametrize("order", [3, 5])
+@pytest.mark.parametrize("variant", [-1, 0, 3])
+@pytest.mark.parametrize("n", [61, 100])
+def test_2d_c128_matches_oracle(gpu, oracle_lib, order, variant, n):
+    s = _spec_2d(n, order)
+    iters = 130
+    want = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float64)
+    got = _device_solve(gpu, s, iters, np.complex128, variant)
+    assert rel(got, want) <= 1e-10
+
+
+def test_2d_plain_config_full(gpu, oracle_lib):
+    """256 x 256 on [-20, 20]^2, ring pump, order 3, dt 5e-5, 20 000 steps via solve_nls_2d."""
+    from nls_gb300 import workloads as w
+    from nls_gb300.native import nls
+    s, steps = w.plain_2d()
+    got = nls.solve_nls_2d(s.dt, s.dx, s.order, steps, s.pumping, s.coeffs, s.u0)
+    want = oracle_lib.solve(s.dt, s.dx, s.order, steps, s.pumping, s.coeffs, s.u0, dtype=np.float64,
+                            threads=os.cpu_count() or 1)
+    assert rel(got, want) <= 1e-10
+
+
+def test_golden_restatement_fixtures(gpu):
+    """GPU against the scipy-BLAS restatement fixtures (both precisions)."""
+    from nls_gb300.native import nls
+    fx = dict(np.load(os.path.join(GOLDEN, "restatement_small.npz")))
+    n, dx, dt, iters, n2, dx2, dt2, iters2 = fx["params"]
+    for order in (3, 5, 7):
+        got = nls.solve_nls(dt, dx, order, int(iters), fx["p1d"], fx["coeffs"], fx["u1d_0"])
+        assert rel(got, fx[f"u1d_o{order}_f64"]) <= 1e-10
+        got = nls.solve_nls(dt, dx, order, int(iters), fx["p1d"], fx["coeffs"], fx["u1d_0"].astype(np.complex64))
+        assert rel(got, fx[f"u1d_o{order}_f32"]) <= 3e-5
+    for order in (3, 5):
+        got = nls.solve_nls_2d(dt2, dx2, order, int(iters2), fx["p2d"], fx["coeffs"], fx["u2d_0"])
+        assert rel(got, fx[f"u2d_o{order}_f64"]) <= 1e-10
+        got = nls.solve_nls_2d(dt2, dx2, order, int(iters2), fx["p2d"], fx["coeffs"], fx["u2d_0"].astype(np.complex64))
+        assert rel(got, fx[f"u2d_o{order}_f32"]) <= 3e-5
+
+
+def test_chemical_potential_matches_oracle(gpu, oracle_lib):
+    from nls_gb300.native import nls
+    s = _spec_1d(300, 5)
+    u = s.u0 * 100 + 0.05
+    mu = nls.chemical_potential_1d(s.dx, s.pumping, s.coeffs, u)
+    want = oracle_lib.chemical_potential(s.dx, s.pumping, s.coeffs, u, dtype=np.float64)
+    assert abs(mu - want) <= 1e-10 * abs(want)
+    s2 = _spec_2d(48, 5)
+    u2 = s2.u0 * 100 + 0.05
+    mu2 = nls.chemical_potential_2d(s2.dx, s2.pumping, s2.coeffs, u2)
+    want2 = oracle_lib.chemical_potential(s2.dx, s2.pumping, s2.coeffs, u2, dtype=np.float64)
+    assert abs(mu2 - want2) <= 1e-10 * abs(want2)
+
+
+# ------------------------------------------------------------------ complex64 precision form
+
+@pytest.mark.parametrize("order", [3, 5, 7])
+@pytest.mark.parametrize("variant", [-1, 1, 2, 0])
+def test_1d_c64_vs_oracles(gpu, oracle_lib, order, variant):
+    s = _spec_1d(700, order)
+    iters = 2000
+    want32 = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float32)
+    want64 = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float64)
+    got = _device_solve(gpu, s, iters, np.complex64, variant)
+    assert rel(got, want32) <= 3e-5
+    assert rel(np.abs(got) ** 2, np.abs(want64) ** 2) <= 1e-4
+
+
+@pytest.mark.parametrize("order", [3, 5])
+@pytest.mark.parametrize("variant", [-1, 0, 1, 2, 3])
+def test_2d_c64_vs_oracles(gpu, oracle_lib, order, variant):
+    s = _spec_2d(150, order)
+    iters = 400
+    want32 = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float32, threads=8)
+    want64 = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float64, threads=8)
+    got = _device_solve(gpu, s, iters, np.complex64, variant)
+    assert rel(got, want32) <= 3e-5
+    d64 = np.abs(want64) ** 2
+    assert rel(np.abs(got) ** 2, d64) <= 1e-4
+    c = s.coeffs
+    n_got = c[11] * s.pumping / (c[12] + c[13] * np.abs(got) ** 2)
+    n_want = c[11] * s.pumping / (c[12] + c[13] * d64)
+    assert rel(n_got, n_want) <= 1e-4
+
+
+def test_device_error_reductions(gpu):
+    import torch
+    from nls_gb300 import device
+    rng = np.random.default_rng(1)
+    a = rng.standard_normal(5000) + 1j * rng.standard_normal(5000)
+    b = a * (1 + 1e-3 * rng.standard_normal(5000))
+    P = rng.random(5000)
+    c = np.zeros(23)
+    c[11], c[12], c[13] = 1.0, 1.0, 0.7
+    ta = torch.tensor(a.astype(np.complex64), device="cuda")
+    tb = torch.tensor(b, device="cuda")
+    tP = torch.tensor(P, device="cuda")
+    d, r = device.density_errors(ta, tb, tP, c)
+    a32 = a.astype(np.complex64).astype(np.complex128)
+    np.testing.assert_allclose(d, rel(np.abs(a32) ** 2, np.abs(b) ** 2), rtol=1e-9)
+    na = P / (1 + 0.7 * np.abs(a32) ** 2)
+    nb = P / (1 + 0.7 * np.abs(b) ** 2)
+    np.testing.assert_allclose(r, rel(na, nb), rtol=1e-9)
+    np.testing.assert_allclose(device.norm(tb), np.sum(np.abs(b) ** 2), rtol=1e-12)
+
+
+def test_nonfinite_state_is_reported(gpu):
+    import torch
+    from nls_gb300 import _lib, device
+    u = torch.zeros(1000, dtype=torch.complex128, device="cuda")
+    u[17] = complex(float("nan"), 0.0)
+    with pytest.raises(_lib.NativeError) as ei:
+        device.norm(u)
+    assert ei.value.status == _lib.NLS_ERR_NONFINITE
+
+
+# ------------------------------------------------------------------ edge cases
+
+def test_edge_sizes_and_iteration_counts(gpu, oracle_lib):
+    from nls_gb300.native import nls
+    for order in (3, 5, 7):
+        s = _spec_1d(order, order, dx=0.3)            # smallest grid the operator allows
+        for iters in (0, 1, 7):
+            want = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float64)
+            got = nls.solve_nls(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0)
+            assert rel(got, want) <= 1e-10 if np.linalg.norm(want) else np.array_equal(got, want)
+    for order in (3, 5):
+        for n in (order, 33, 57):
+            s = _spec_2d(n, order)
+            for iters in (0, 1, 65):
+                want = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float64)
+                got = nls.solve_nls_2d(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0)
+                assert rel(got, want) <= 1e-10
+
+
+def test_invalid_arguments_raise(gpu):
+    from nls_gb300.native import nls
+    s = _spec_1d(64, 5)
+    with pytest.raises(ValueError):
+        nls.solve_nls(s.dt, s.dx, 4, 10, s.pumping, s.coeffs, s.u0)
+    s2 = _spec_2d(16, 3)
+    with pytest.raises(ValueError):
+        nls.solve_nls_2d(s2.dt, s2.dx, 7, 10, s2.pumping, s2.coeffs, s2.u0)
+
+
+# ------------------------------------------------------------------ resume, batch, pool
+
+@pytest.mark.parametrize("dim,variant,dtype", [(1, -1, np.complex128), (1, 0, np.complex64),
+                                               (2, 1, np.complex64), (2, 0, np.complex128),
+                                               (2, 3, np.complex128)])
+def test_resume_is_bitwise(gpu, dim, variant, dtype):
+    """One solve of N steps equals k solves of N/k steps from the device-resident state."""
+    import torch
+    from nls_gb300 import device
+    s = _spec_1d(300, 5) if dim == 1 else _spec_2d(90, 3)
+    ct = torch.complex128 if dtype == np.complex128 else torch.complex64
+    rt = torch.float64 if dtype == np.complex128 else torch.float32
+    P = torch.tensor(np.ascontiguousarray(s.pumping), dtype=rt, device="cuda")
+    u1 = torch.tensor(np.ascontiguousarray(s.u0), dtype=ct, device="cuda")
+    u2 = u1.clone()
+    device.solve_(u1, P, order=s.order, dt=s.dt, dx=s.dx, coeffs=s.coeffs, iters=195, variant=variant)
+    for _ in range(3):
+        device.solve_(u2, P, order=s.order, dt=s.dt, dx=s.dx, coeffs=s.coeffs, iters=65, variant=variant)
+    assert torch.equal(u1, u2)
+
+
+def _mixed_specs(dtype):
+    from nls_gb300 import workloads as w
+    specs = [w.mix_instance(i, 1) for i in range(5)] + [w.mix_instance(10 + i, 2) for i in range(6)]
+    # include sizes that are not multiples of any tile and the smallest allowed sides
+    extra = _spec_2d(37, 3)
+    extra.variant = 3
+    specs.append(extra)
+    return specs
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_batch_matches_single_solves(gpu, dtype):
+    from nls_gb300.batch import BatchSolver
+    specs = _mixed_specs(dtype)
+    b = BatchSolver(specs, dtype=dtype)
+    b.run(57)
+    b.run(20)
+    for i, s in enumerate(specs):
+        got = b.get(i)
+        want = _device_solve(gpu, s, 77, dtype, s.variant)
+        assert np.array_equal(got, want.astype(got.dtype)), i
+
+
+def test_pool_same_alone_and_in_the_mix(gpu):
+    from nls_gb300 import workloads as w
+    from nls_gb300.serve import Pool
+    target = w.mix_instance(3, 2)
+    target1 = w.mix_instance(4, 1)
+    alone = Pool(budget_bytes=1 << 30, chunk_steps=40)
+    alone.admit(target, 123, 0)
+    alone.admit(target1, 77, 1)
+    while alone.status()[0]:
+        alone.step()
+    ra = dict([alone.take_with_state(), alone.take_with_state()])
+    mix = Pool(budget_bytes=1 << 30, chunk_steps=40)
+    others = [w.mix_instance(20 + i, 1 + (i % 2)) for i in range(8)]
+    for k, o in enumerate(others[:4]):
+        mix.admit(o, 50 + 13 * k, 100 + k)
+    mix.step()                                   # the target arrives while others run
+    mix.admit(target, 123, 0)
+    for k, o in enumerate(others[4:]):
+        mix.admit(o, 90 + 7 * k, 200 + k)
+    mix.step()
+    mix.admit(target1, 77, 1)
+    rm = {}
+    while True:
+        got = mix.take_with_state()
+        if got is not None:
+            rm[got[0]] = got[1]
+            continue
+        if mix.status()[0] == 0:
+            break
+        mix.step()
+    assert np.array_equal(ra[0], rm[0])
+    assert np.array_equal(ra[1], rm[1])
+    # and equal to a plain single solve on the same kernel
+    want = _device_solve(gpu, target, 123, np.complex64, -1)
+    assert np.array_equal(rm[0], want)
