@@ -30,7 +30,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "node-steps/s batched FP32 vs plain FP64 GPU at relL2≤1e-4; serve p50/p99 ms"
 UNIT = "node-steps/s"
-SOLVE_STEPS = 5000
+SOLVE_STEPS = 5000  # RK4 steps per solve of the batched mix (the --solve-steps default)
 # Algorithmic HBM bytes per node-step of the fused single-pass 2-D step (complex64 state read and
 # written once, float32 pump read once): 8 + 4 + 8.
 BYTES_PER_NODE_STEP_C64 = 20
@@ -166,6 +166,12 @@ def oracle_sample(specs):
     return [s for i, s in enumerate(specs) if i % 4 == 0]
 
 
+def calibrated_steps(specs, threads, target_s=12.0):
+    """RK4 steps per CPU sample so that one sample takes about target_s seconds."""
+    _, t1 = cpu_oracle_rate(specs, 1, threads)
+    return int(min(2000, max(1, round(target_s / max(t1, 1e-3)))))
+
+
 def run_reference(args):
     """--impl reference: the reference algorithm on the host cores (the oracle port), same metric."""
     ws, rank, local = dist_init()
@@ -174,9 +180,9 @@ def run_reference(args):
     from nls_gb300 import workloads
     specs = oracle_sample(workloads.batch_mix())
     threads = os.cpu_count() or 1
-    steps = 4
     for _ in range(args.warmup):
         cpu_oracle_rate(specs[:8], 1, threads)
+    steps = calibrated_steps(specs, threads, target_s=15.0)
     rates, times = [], []
     for _ in range(args.steps):
         r, t = cpu_oracle_rate(specs, steps, threads)
@@ -201,6 +207,46 @@ def run_reference(args):
 
 # ------------------------------------------------------------------ GPU legs
 
+def run_grid(args):
+    """--workload grid1d|grid2d: one solve of one grid (profiling and single-solve roofline)."""
+    import torch
+    ws, rank, local = dist_init()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    from nls_gb300 import build as nbuild
+    nbuild.build()
+    from nls_gb300 import device as ndev
+    from nls_gb300 import workloads
+    dtype = np.complex128 if args.c128 else np.complex64
+    if args.workload == "grid2d":
+        s, _ = workloads.plain_2d(n=args.n, length=args.n * 0.15625, order=args.order)
+    else:
+        s, _ = workloads.plain_1d(n=args.n, length=args.n * 0.04, order=args.order)
+    ct = torch.complex128 if args.c128 else torch.complex64
+    rt = torch.float64 if args.c128 else torch.float32
+    u = torch.tensor(np.ascontiguousarray(s.u0), dtype=ct, device=dev)
+    P = torch.tensor(np.ascontiguousarray(s.pumping), dtype=rt, device=dev)
+    kw = dict(order=s.order, dt=s.dt, dx=s.dx, coeffs=s.coeffs, variant=args.variant)
+    for _ in range(args.warmup):
+        ndev.solve_(u, P, iters=args.solve_steps, **kw)
+    ext = ndev.stream(local)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(args.steps):
+        ndev.solve_(u, P, iters=args.solve_steps, **kw)
+    e1.record(ext)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    ns = float(s.nodes) * args.solve_steps * args.steps
+    bpn = 40 if args.c128 else 20
+    print(json.dumps({"workload": args.workload, "n": args.n, "order": args.order, "dtype": np.dtype(dtype).name,
+                      "variant": args.variant, "node_steps_per_s": ns / (ms / 1e3),
+                      "us_per_rk4_step": ms * 1e3 / (args.solve_steps * args.steps),
+                      "algorithmic_GBps": ns * bpn / (ms / 1e3) / 1e9}))
+    return 0
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_init()
@@ -220,8 +266,9 @@ def run_ours(args):
     ext = ndev.stream(local)
 
     # warm-up: includes graph capture/instantiation for SOLVE_STEPS
+    steps_per_solve = args.solve_steps
     for _ in range(args.warmup):
-        b.run(SOLVE_STEPS)
+        b.run(steps_per_solve)
     b.synchronize()
 
     launches0 = ndev.launches(local)
@@ -231,7 +278,7 @@ def run_ours(args):
     with ClockSampler(local) as clk:
         e0.record(ext)
         for _ in range(args.steps):
-            b.run(SOLVE_STEPS)
+            b.run(steps_per_solve)
         e1.record(ext)
         e1.synchronize()
     torch.cuda.synchronize(dev)
@@ -239,7 +286,7 @@ def run_ours(args):
     ms = e0.elapsed_time(e1)
     gpu_launches = ndev.launches(local) - launches0
     ms = max_over_ranks(ws, ms, dev)
-    node_steps = float(total_nodes) * SOLVE_STEPS * args.steps * ws
+    node_steps = float(total_nodes) * steps_per_solve * args.steps * ws
     value = node_steps / (ms / 1e3)
     clocks = clk.summary()
 
@@ -249,7 +296,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "complex64", "data": "synthetic (seeded)",
         "config": {"workload": "batch_mix: 256 radial grids (500-8192 nodes, order 5) + 256 square grids "
                                "(64-512 per side, order 3), 5000 RK4 steps each, complex64",
-                   "instances": len(specs), "steps_per_solve": SOLVE_STEPS, "total_nodes": total_nodes,
+                   "instances": len(specs), "steps_per_solve": steps_per_solve, "total_nodes": total_nodes,
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                    "l2": "inputs larger than L2 (2-D states + pumps ~%.0f MB per step)" %
                          (nodes_2d * BYTES_PER_NODE_STEP_C64 / 1e6)},
@@ -257,6 +304,9 @@ def run_ours(args):
         "clocks": clocks,
     }
     if rank != 0:
+        return 0
+    if args.quick:
+        print(json.dumps(result))
         return 0
 
     # ---- roofline of the fused 2-D step kernel (the dominant kernel), timed alone on its stream
@@ -354,10 +404,12 @@ def run_ours(args):
     if not args.no_cpu:
         threads = os.cpu_count() or 1
         samp = oracle_sample(specs)
-        rate, secs = cpu_oracle_rate(samp, 4, threads)
+        csteps = calibrated_steps(samp, threads)
+        rate, secs = cpu_oracle_rate(samp, csteps, threads)
         result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                  "sample": f"every 4th of the 512 instances ({len(samp)} solves) x 4 RK4 steps, "
-                                            f"float32 C++ restatement of nls/nls.f90, {secs:.1f} s"}
+                                  "sample": f"every 4th of the 512 instances ({len(samp)} solves) x {csteps} RK4 "
+                                            f"steps, float32 C++ restatement of nls/nls.f90 (OpenMP over 2-D "
+                                            f"columns), {secs:.1f} s"}
     print(json.dumps(result))
     return 0
 
@@ -370,9 +422,19 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--serve", type=int, default=400, help="requests in the served stream (0 = skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
+    ap.add_argument("--quick", action="store_true",
+                    help="timed batched solves only (no roofline, accuracy, e2e, serve or CPU legs)")
+    ap.add_argument("--workload", choices=["batch", "grid1d", "grid2d"], default="batch")
+    ap.add_argument("--solve-steps", type=int, default=SOLVE_STEPS, help="RK4 steps per solve")
+    ap.add_argument("--n", type=int, default=4096, help="grid size for grid1d/grid2d")
+    ap.add_argument("--order", type=int, default=3, help="stencil order for grid1d/grid2d")
+    ap.add_argument("--variant", type=int, default=-1, help="kernel variant for grid1d/grid2d")
+    ap.add_argument("--c128", action="store_true", help="complex128 state for grid1d/grid2d")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "batch":
+        return run_grid(args)
     return run_ours(args)
 
 

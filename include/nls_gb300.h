@@ -45,7 +45,8 @@ typedef struct nls_pool nls_pool;
 /* One solve: dim 1 is the radial 1-D model of solve_nls (nls/nls.f90:797-813), dim 2 the
  * Cartesian model of solve_nls_2d (nls/nls.f90:903-919).  variant selects a kernel shape chosen by
  * the autotuner (-1 = built-in choice): 1-D = CTAs per solve (cluster size 1..16, 0 = unfused
- * stage kernels); 2-D = 0 unfused, 1 tile 64x64, 2 tile 128x32, 3 tile 32x32. */
+ * stage kernels); 2-D = 0 unfused, or a fused tile region (threads): 1 = 64x64 (512),
+ * 2 = 128x32 (512), 3 = 32x32 (256), 4 = 64x64 (1024), 5 = 128x32 (1024). */
 typedef struct nls_problem {
   int dim;
   int n;
@@ -152,6 +153,7 @@ int nls_pool_take(nls_pool* pool, int64_t* tag, void* u, size_t u_bytes);
 /* Admitted-but-unfinished requests, bytes of budget in use. */
 int nls_pool_status(nls_pool* pool, int* active, size_t* bytes_in_use);
 int nls_pool_destroy(nls_pool* pool);
+
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,119 @@
+"""Project-written autotuner for kernel shape and stage fusion.
+
+For each (dimension, precision, stencil order, grid-size bucket) it times the candidate kernel
+variants on a seeded instance of that size and keeps the fastest:
+
+* 2-D: 0 = unfused (four stage launches per step, no halo recomputation), or a fused
+  single-pass step with tile region 64x64 / 512 threads (1), 128x32 / 512 (2), 32x32 / 256 (3),
+  64x64 / 1024 (4) or 128x32 / 1024 (5);
+* 1-D: the resident kernel on 1, 2, 4, 8 or 16 CTAs of a cluster, or 0 = unfused stage kernels.
+
+Results are cached per GPU name in a JSON file (``NLS_GB300_TUNE_CACHE`` or
+``~/.cache/nls_gb300/autotune.json``); ``apply(specs, dtype)`` fills ``Spec.variant`` for a
+batch.  Timings use CUDA events on the library's stream.
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import threading
+
+import numpy as np
+
+_lock = threading.Lock()
+
+
+def _cache_path():
+    return os.environ.get("NLS_GB300_TUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "nls_gb300", "autotune.json"))
+
+
+def bucket(n: int) -> int:
+    """Size bucket: the next power of two (for 2-D, of the side)."""
+    b = 1
+    while b < n:
+        b *= 2
+    return b
+
+
+def candidates(dim: int, dtype, n: int):
+    c64 = np.dtype(dtype) == np.dtype(np.complex64)
+    if dim == 2:
+        return [1, 2, 3, 4, 5, 0] if c64 else [0, 3]
+    out = []
+    lim = 4096 if c64 else 2048
+    for cl in (1, 2, 4, 8, 16):
+        seg = -(-n // cl)
+        if seg <= lim and seg >= 6:
+            out.append(cl)
+    return out + [0]
+
+
+def _time_variant(dim, n, order, dtype, variant, steps, device):
+    import torch
+
+    from . import device as ndev
+    from . import workloads
+    if dim == 2:
+        s, _ = workloads.plain_2d(n=n, length=n * 0.15625, order=order)
+    else:
+        s, _ = workloads.plain_1d(n=n, length=n * 0.04, order=order)
+    ct = torch.complex64 if np.dtype(dtype) == np.dtype(np.complex64) else torch.complex128
+    rt = torch.float32 if ct == torch.complex64 else torch.float64
+    u = torch.tensor(np.ascontiguousarray(s.u0), dtype=ct, device=f"cuda:{device}")
+    P = torch.tensor(np.ascontiguousarray(s.pumping), dtype=rt, device=f"cuda:{device}")
+    kw = dict(order=order, dt=s.dt, dx=s.dx, coeffs=s.coeffs, variant=variant)
+    ndev.solve_(u, P, iters=steps, **kw)           # warm-up (graph instantiation, attributes)
+    ext = ndev.stream(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    ndev.solve_(u, P, iters=steps, **kw)
+    e1.record(ext)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def tune(dim: int, n: int, order: int, dtype=np.complex64, steps: int = 128, device: int = 0):
+    """Fastest variant for this case (cached)."""
+    import torch
+    name = torch.cuda.get_device_name(device)
+    key = f"{name}|{dim}|{np.dtype(dtype).name}|{order}|{bucket(n)}"
+    path = _cache_path()
+    with _lock:
+        cache = {}
+        if os.path.exists(path):
+            try:
+                with open(path) as f:
+                    cache = json.load(f)
+            except (OSError, ValueError):
+                cache = {}
+        if key in cache:
+            return int(cache[key]["variant"])
+    times = {}
+    nb = bucket(n)
+    for v in candidates(dim, dtype, nb):
+        try:
+            times[v] = _time_variant(dim, nb, order, dtype, v, steps, device)
+        except ValueError:
+            continue
+    best = min(times, key=times.get)
+    with _lock:
+        cache[key] = {"variant": int(best), "ms_per_step": {str(k): t for k, t in times.items()}}
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(cache, f, indent=1)
+        os.replace(tmp, path)
+    return int(best)
+
+
+def apply(specs, dtype=np.complex64, device: int = 0):
+    """Set each Spec.variant from the tuned choice for its size bucket; returns the specs."""
+    memo = {}
+    for s in specs:
+        k = (s.dim, s.order, bucket(s.n))
+        if k not in memo:
+            memo[k] = tune(s.dim, s.n, s.order, dtype=dtype, device=device)
+        s.variant = memo[k]
+    return specs

@@ -2,9 +2,10 @@
 //
 // rk4_2d_fused: one launch applies one complete RK4 step (the four `hamiltonian_2d` calls and the
 // update of `runge_kutta_2d`, nls/nls.f90:892-900) to a list of tiles.  A CTA stages its tile plus
-// a halo of 4K nodes (K = 1 for order 3, 2 for order 5) in shared memory, evaluates stage s on the
-// region shrunk by s*K, keeps u, the pump and the RK4 accumulator of its nodes in registers, and
-// writes only the new state: per node-step HBM sees one read of u and P and one write of u.  The
+// a halo of 4K nodes (K = 1 for order 3, 2 for order 5) in shared memory, evaluates the four stages
+// back to back (stage s is valid on the region shrunk by s*K), keeps u, the pump and the RK4
+// accumulator of its nodes in registers, and writes only the new state: per node-step HBM sees
+// one read of u and P and one write of u.  The
 // tile list may span many independent solves (batched and served forms), each with its own size,
 // coefficients and ping-pong buffers; the persistent grid strides over the list.
 //
@@ -21,23 +22,111 @@ __device__ __forceinline__ typename C2<T>::type cadd4(typename C2<T>::type a, ty
   return mk<T>((a.x + b.x) + (c.x + d.x), (a.y + b.y) + (c.y + d.y));
 }
 
-template <typename T, int K, int RX, int RY, int NT>
-__global__ void __launch_bounds__(NT, 2)
+// Complex pair arithmetic: Blackwell's packed FP32x2 pipe (FADD2/FMUL2/FFMA2) for complex64,
+// plain FP64 for complex128.
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float s, float2 b, float2 c) { return __ffma2_rn(make_float2(s, s), b, c); }
+__device__ __forceinline__ float2 pmul(float s, float2 b) { return __fmul2_rn(make_float2(s, s), b); }
+__device__ __forceinline__ double2 padd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 pfma(double s, double2 b, double2 c) {
+  return make_double2(fma(s, b.x, c.x), fma(s, b.y, c.y));
+}
+__device__ __forceinline__ double2 pmul(double s, double2 b) { return make_double2(s * b.x, s * b.y); }
+
+// Right-hand side with the pump already multiplied by c12 (the reference evaluates
+// coeffs(12) * pumping first, nls/nls.f90:580, so folding it changes no rounding).
+template <typename T>
+__device__ __forceinline__ typename C2<T>::type rhs_pc(typename C2<T>::type u, T pc,
+                                                       typename C2<T>::type lu, const Phys<T>& ph) {
+  const T s = fma(u.x, u.x, u.y * u.y);
+  const T r = rdiv(pc, fma(ph.c14, s, ph.c13));
+  const T a = fma(ph.c3, r, -ph.c4);
+  const T b = fma(ph.c5, s, ph.c6 * r);
+  typename C2<T>::type v;
+  v.x = fma(a, u.x, fma(b, u.y, -lu.y));
+  v.y = fma(a, u.y, fma(-b, u.x, lu.x));
+  return v;
+}
+
+// Tile geometry: a region of RX x RY nodes (the output tile plus a halo of H = 4K on every
+// side) computed by (RX/32) x NS warps; warp (xw, strip) owns columns xw*32 .. xw*32+31 of rows
+// strip*NJ .. strip*NJ+NJ-1, so every branch below is warp-uniform.
+template <typename T, int K, int RX, int RY, int NS>
+struct TileCfg {
+  static constexpr int WX = RX / 32;
+  static constexpr int NT = WX * NS * 32;
+  static constexpr int NJ = RY / NS;
+  static constexpr int H = 4 * K;
+  static constexpr int TX = RX - 2 * H;
+  static constexpr int TY = RY - 2 * H;
+  static constexpr int ROWS = RY + 2 * K;     // K guard rows above and below each buffer
+  static constexpr size_t SMEM = (size_t)2 * ROWS * RX * sizeof(typename C2<T>::type);
+  // CTAs per SM the register budget is sized for: 2 x 256 threads, else one CTA
+  static constexpr int MINB = NT <= 256 ? 2 : 1;
+  static_assert(RX % 32 == 0 && RY % NS == 0 && NJ <= 32, "tile layout");
+  static_assert(TX > 0 && TY > 0, "tile too small for its halo");
+};
+
+// One RK4 stage S over the thread's column strip.  Every node of the region is evaluated (the
+// stage's valid region shrinks by K per stage; values computed outside it are never read again),
+// and only in-domain nodes are stored, so out-of-domain halo stays exactly zero.
+template <typename T, int K, int RX, int NJ, int S>
+__device__ __forceinline__ void tile_stage(const typename C2<T>::type* __restrict__ in,
+                                           typename C2<T>::type* __restrict__ out, int x, int y0,
+                                           typename C2<T>::type (&u)[NJ], typename C2<T>::type (&acc)[NJ],
+                                           const T (&pc)[NJ], unsigned dom, const Phys<T>& ph,
+                                           const RK<T>& rk, T wc, T w1, T w2) {
+  typedef typename C2<T>::type C;
+  C w[2 * K + 1];
+#pragma unroll
+  for (int d = 0; d <= 2 * K; ++d) w[d] = in[(y0 - K + d) * RX + x];
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const int c = (y0 + j) * RX + x;
+    const C v = w[K];
+    C s1 = padd(padd(in[c - 1], in[c + 1]), padd(w[K - 1], w[K + 1]));
+    C lu = pfma(w1, s1, pmul(wc, v));
+    if (K == 2) {
+      C s2 = padd(padd(in[c - 2], in[c + 2]), padd(w[0], w[2 * K]));
+      lu = pfma(w2, s2, lu);
+    }
+    const C k = rhs_pc<T>(v, pc[j], lu, ph);
+    if (S == 1) acc[j] = k;
+    else acc[j] = pfma(S == 4 ? (T)1 : (T)2, k, acc[j]);
+    if (S < 4) {
+      const C t = pfma(S == 3 ? rk.dt : rk.half_dt, k, u[j]);
+      if (dom & (1u << j)) out[c] = t;
+    } else {
+      u[j] = pfma(rk.dt6, acc[j], u[j]);
+    }
+#pragma unroll
+    for (int d = 0; d < 2 * K; ++d) w[d] = w[d + 1];
+    if (j + 1 < NJ) w[2 * K] = in[(y0 + j + 1 + K) * RX + x];
+  }
+}
+
+template <typename T, int K, int RX, int RY, int NS>
+__global__ void __launch_bounds__(TileCfg<T, K, RX, RY, NS>::NT, TileCfg<T, K, RX, RY, NS>::MINB)
 rk4_2d_fused(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items, int n_items,
              int j_step) {
   typedef typename C2<T>::type C;
-  constexpr int H = 4 * K;
-  constexpr int TX = RX - 2 * H;
-  constexpr int TY = RY - 2 * H;
-  constexpr int G = NT / RX;
-  constexpr int NJ = RY / G;
-  static_assert(NT % RX == 0 && RY % G == 0, "thread layout");
-  static_assert(TX > 0 && TY > 0, "tile too small for halo");
+  typedef TileCfg<T, K, RX, RY, NS> G;
+  constexpr int NJ = G::NJ, H = G::H;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* bufA = reinterpret_cast<C*>(smem_raw);
-  C* bufB = bufA + RX * RY;
-  const int x = threadIdx.x % RX;
-  const int g = threadIdx.x / RX;
+  C* base = reinterpret_cast<C*>(smem_raw);
+  C* buf0 = base + K * RX;                   // row 0 of buffer 0 (rows -K .. RY+K-1 exist)
+  C* buf1 = base + G::ROWS * RX + K * RX;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int x = (warp % G::WX) * 32 + lane;
+  const int y0 = (warp / G::WX) * NJ;
+  // guard rows are read by the edge rows' stencils and never written: zero them once
+  for (int i = threadIdx.x; i < K * RX; i += G::NT) {
+    buf0[-K * RX + i] = mk<T>(0, 0);
+    buf0[RY * RX + i] = mk<T>(0, 0);
+    buf1[-K * RX + i] = mk<T>(0, 0);
+    buf1[RY * RX + i] = mk<T>(0, 0);
+  }
+  const bool x_interior = x >= H && x < RX - H;
 
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const TileItem ti = items[it];
@@ -50,69 +139,46 @@ rk4_2d_fused(const Inst2D* __restrict__ insts, const TileItem* __restrict__ item
     const T* __restrict__ Pg = reinterpret_cast<const T*>(I.P);
     const int tyi = ti.tile / I.tiles_x;
     const int txi = ti.tile - tyi * I.tiles_x;
-    const int gx = txi * TX - H + x;
-    const int gy0 = tyi * TY - H;
+    const int gx = txi * G::TX - H + x;
+    const int gy0 = tyi * G::TY - H + y0;
     const bool xin = gx >= 0 && gx < n;
     const Phys<T> ph = phys_from<T>(I.ph);
     const RK<T> rk = rk_from<T>(I.dt);
     const T wc = (T)I.op.center, w1 = (T)I.op.w[0], w2 = (T)I.op.w[1];
+    const T c12 = (T)I.ph.c12;
 
     C u[NJ], acc[NJ];
-    T P[NJ];
+    T pc[NJ];
+    unsigned dom = 0, store = 0;
 #pragma unroll
     for (int j = 0; j < NJ; ++j) {
-      const int y = g + G * j;
-      const int gy = gy0 + y;
+      const int gy = gy0 + j;
       const bool inb = xin && gy >= 0 && gy < n;
       const size_t q = (size_t)gy * n + gx;
       u[j] = inb ? src[q] : mk<T>(0, 0);
-      P[j] = inb ? Pg[q] : (T)0;
+      pc[j] = inb ? c12 * Pg[q] : (T)0;
       acc[j] = mk<T>(0, 0);
-      bufA[y * RX + x] = u[j];
+      dom |= (unsigned)inb << j;
+      const int y = y0 + j;
+      store |= (unsigned)(inb && x_interior && y >= H && y < RY - H) << j;
+    }
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      buf0[(y0 + j) * RX + x] = u[j];
+      if (!(dom & (1u << j))) buf1[(y0 + j) * RX + x] = mk<T>(0, 0);
     }
     __syncthreads();
-
-#pragma unroll 1
-    for (int s = 1; s <= 4; ++s) {
-      const C* in = (s & 1) ? bufA : bufB;
-      C* out = (s & 1) ? bufB : bufA;
-      const int lo = s * K;
-      const bool xact = x >= lo && x < RX - lo;
-      const T coef = s == 3 ? rk.dt : rk.half_dt;
-      const T wk = (s == 1 || s == 4) ? (T)1 : (T)2;
+    tile_stage<T, K, RX, NJ, 1>(buf0, buf1, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
+    __syncthreads();
+    tile_stage<T, K, RX, NJ, 2>(buf1, buf0, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
+    __syncthreads();
+    tile_stage<T, K, RX, NJ, 3>(buf0, buf1, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
+    __syncthreads();
+    tile_stage<T, K, RX, NJ, 4>(buf1, nullptr, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
 #pragma unroll
-      for (int j = 0; j < NJ; ++j) {
-        const int y = g + G * j;
-        if (xact && y >= lo && y < RY - lo) {
-          const int c = y * RX + x;
-          const C v = in[c];
-          const C s1 = cadd4<T>(in[c - 1], in[c + 1], in[c - RX], in[c + RX]);
-          C lu = mk<T>(wc * v.x + w1 * s1.x, wc * v.y + w1 * s1.y);
-          if (K == 2) {
-            const C s2 = cadd4<T>(in[c - 2], in[c + 2], in[c - 2 * RX], in[c + 2 * RX]);
-            lu.x += w2 * s2.x;
-            lu.y += w2 * s2.y;
-          }
-          const C k = rhs<T>(v, P[j], lu, ph);
-          if (s == 1) {
-            acc[j] = k;
-          } else {
-            acc[j].x += wk * k.x;
-            acc[j].y += wk * k.y;
-          }
-          const int gy = gy0 + y;
-          const bool inb = xin && gy >= 0 && gy < n;
-          if (s < 4) {
-            C t = mk<T>(u[j].x + coef * k.x, u[j].y + coef * k.y);
-            if (!inb) t = mk<T>(0, 0);
-            out[c] = t;
-          } else if (inb) {
-            dst[(size_t)gy * n + gx] = mk<T>(u[j].x + rk.dt6 * acc[j].x, u[j].y + rk.dt6 * acc[j].y);
-          }
-        }
-      }
-      if (s < 4) __syncthreads();
-    }
+    for (int j = 0; j < NJ; ++j)
+      if (store & (1u << j)) dst[(size_t)(gy0 + j) * n + gx] = u[j];
+    __syncthreads();  // the next tile's load rewrites both buffers
   }
 }
 
@@ -194,63 +260,75 @@ __global__ void __launch_bounds__(256) rhs_2d(int n, const void* __restrict__ u_
 
 // ------------------------------------------------------------------ launchers
 
+// Shape table: region RX x RY computed by (RX/32) x NS warps.
+//   TILE_64x64   : 64 x 64,  8 strips of 8 rows  (512 threads)
+//   TILE_128x32  : 128 x 32, 4 strips of 8 rows  (512 threads)
+//   TILE_32x32   : 32 x 32,  8 strips of 4 rows  (256 threads)
+//   TILE_64x64W  : 64 x 64,  16 strips of 4 rows (1024 threads)
+//   TILE_128x32W : 128 x 32, 8 strips of 4 rows  (1024 threads)
 int tile_region_x(int shape) {
-  switch (shape) { case TILE_64x64: return 64; case TILE_128x32: return 128; case TILE_32x32: return 32; }
+  switch (shape) {
+    case TILE_64x64: return 64; case TILE_128x32: return 128; case TILE_32x32: return 32;
+    case TILE_64x64W: return 64; case TILE_128x32W: return 128;
+  }
   return 0;
 }
 int tile_region_y(int shape) {
-  switch (shape) { case TILE_64x64: return 64; case TILE_128x32: return 32; case TILE_32x32: return 32; }
+  switch (shape) {
+    case TILE_64x64: return 64; case TILE_128x32: return 32; case TILE_32x32: return 32;
+    case TILE_64x64W: return 64; case TILE_128x32W: return 32;
+  }
   return 0;
 }
 int tile_out_x(int shape, int K) { return tile_region_x(shape) - 8 * K; }
 int tile_out_y(int shape, int K) { return tile_region_y(shape) - 8 * K; }
 bool tile_supported(int shape, int dtype) {
   if (shape == TILE_32x32) return true;
-  if (shape == TILE_64x64 || shape == TILE_128x32) return dtype == NLS_C64;
+  if (shape == TILE_64x64 || shape == TILE_128x32 || shape == TILE_64x64W || shape == TILE_128x32W)
+    return dtype == NLS_C64;
   return false;
 }
 
-template <typename T, int K, int RX, int RY>
+template <typename T, int K, int RX, int RY, int NS>
 static cudaError_t launch_f(const Inst2D* d_insts, const TileItem* d_items, int n_items, int j_step,
                             int grid, cudaStream_t s) {
-  auto kern = rk4_2d_fused<T, K, RX, RY, 256>;
-  const size_t smem = (size_t)2 * RX * RY * sizeof(typename C2<T>::type);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
-  kern<<<grid, 256, smem, s>>>(d_insts, d_items, n_items, j_step);
+  typedef TileCfg<T, K, RX, RY, NS> G;
+  auto kern = rk4_2d_fused<T, K, RX, RY, NS>;
+  kern<<<grid, G::NT, G::SMEM, s>>>(d_insts, d_items, n_items, j_step);
   return cudaGetLastError();
 }
 
-template <typename T, int K, int RX, int RY>
+// Sets the shared-memory attribute (outside any capture) and returns CTAs per SM.
+template <typename T, int K, int RX, int RY, int NS>
 static int occ_f() {
-  auto kern = rk4_2d_fused<T, K, RX, RY, 256>;
-  const size_t smem = (size_t)2 * RX * RY * sizeof(typename C2<T>::type);
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  typedef TileCfg<T, K, RX, RY, NS> G;
+  auto kern = rk4_2d_fused<T, K, RX, RY, NS>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM) != cudaSuccess)
+    return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, smem) != cudaSuccess) return 1;
-  return nb > 0 ? nb : 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, G::NT, G::SMEM) != cudaSuccess) return 0;
+  return nb;
 }
 
-#define NLSG_SHAPE_DISPATCH(T, K, shape, CALL)                 \
-  switch (shape) {                                            \
-    case TILE_64x64: return CALL<T, K, 64, 64>();             \
-    case TILE_128x32: return CALL<T, K, 128, 32>();           \
-    case TILE_32x32: return CALL<T, K, 32, 32>();             \
+#define NLSG_SHAPES(T, K, CALL, ...)                                        \
+  switch (shape) {                                                         \
+    case TILE_64x64: return CALL<T, K, 64, 64, 8>(__VA_ARGS__);            \
+    case TILE_128x32: return CALL<T, K, 128, 32, 4>(__VA_ARGS__);          \
+    case TILE_32x32: return CALL<T, K, 32, 32, 8>(__VA_ARGS__);            \
+    case TILE_64x64W: return CALL<T, K, 64, 64, 16>(__VA_ARGS__);          \
+    case TILE_128x32W: return CALL<T, K, 128, 32, 8>(__VA_ARGS__);         \
   }
 
 int fused_2d_blocks_per_sm(int dtype, int K, int shape) {
   if (!tile_supported(shape, dtype)) return 0;
   if (dtype == NLS_C128) {
-    if (K == 1) { if (shape == TILE_32x32) return occ_f<double, 1, 32, 32>(); }
-    if (K == 2) { if (shape == TILE_32x32) return occ_f<double, 2, 32, 32>(); }
+    if (shape != TILE_32x32) return 0;
+    if (K == 1) return occ_f<double, 1, 32, 32, 8>();
+    if (K == 2) return occ_f<double, 2, 32, 32, 8>();
     return 0;
   }
-  if (K == 1) { NLSG_SHAPE_DISPATCH(float, 1, shape, occ_f) }
-  if (K == 2) { NLSG_SHAPE_DISPATCH(float, 2, shape, occ_f) }
+  if (K == 1) { NLSG_SHAPES(float, 1, occ_f) }
+  if (K == 2) { NLSG_SHAPES(float, 2, occ_f) }
   return 0;
 }
 
@@ -261,23 +339,12 @@ cudaError_t launch_2d_fused(int dtype, int K, int shape, const Inst2D* d_insts,
   if (!tile_supported(shape, dtype)) return cudaErrorInvalidValue;
   if (dtype == NLS_C128) {
     if (shape != TILE_32x32) return cudaErrorInvalidValue;
-    if (K == 1) return launch_f<double, 1, 32, 32>(d_insts, d_items, n_items, j_step, grid, s);
-    if (K == 2) return launch_f<double, 2, 32, 32>(d_insts, d_items, n_items, j_step, grid, s);
+    if (K == 1) return launch_f<double, 1, 32, 32, 8>(d_insts, d_items, n_items, j_step, grid, s);
+    if (K == 2) return launch_f<double, 2, 32, 32, 8>(d_insts, d_items, n_items, j_step, grid, s);
     return cudaErrorInvalidValue;
   }
-  if (K == 1) {
-    switch (shape) {
-      case TILE_64x64: return launch_f<float, 1, 64, 64>(d_insts, d_items, n_items, j_step, grid, s);
-      case TILE_128x32: return launch_f<float, 1, 128, 32>(d_insts, d_items, n_items, j_step, grid, s);
-      case TILE_32x32: return launch_f<float, 1, 32, 32>(d_insts, d_items, n_items, j_step, grid, s);
-    }
-  } else if (K == 2) {
-    switch (shape) {
-      case TILE_64x64: return launch_f<float, 2, 64, 64>(d_insts, d_items, n_items, j_step, grid, s);
-      case TILE_128x32: return launch_f<float, 2, 128, 32>(d_insts, d_items, n_items, j_step, grid, s);
-      case TILE_32x32: return launch_f<float, 2, 32, 32>(d_insts, d_items, n_items, j_step, grid, s);
-    }
-  }
+  if (K == 1) { NLSG_SHAPES(float, 1, launch_f, d_insts, d_items, n_items, j_step, grid, s) }
+  if (K == 2) { NLSG_SHAPES(float, 2, launch_f, d_insts, d_items, n_items, j_step, grid, s) }
   return cudaErrorInvalidValue;
 }
 

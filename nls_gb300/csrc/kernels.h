@@ -29,9 +29,11 @@ cudaError_t launch_rhs_1d(int dtype, int n, const void* u, const void* P, void* 
 // Fused-step tile shapes (region = tile + halo of 4K on every side).
 enum TileShape2D {
   TILE_UNFUSED = 0,   // four stage launches per step, no halo recomputation
-  TILE_64x64 = 1,     // region 64 x 64, 256 threads (single precision)
-  TILE_128x32 = 2,    // region 128 x 32, 256 threads (single precision)
+  TILE_64x64 = 1,     // region 64 x 64, 512 threads (single precision)
+  TILE_128x32 = 2,    // region 128 x 32, 512 threads (single precision)
   TILE_32x32 = 3,     // region 32 x 32, 256 threads (either precision)
+  TILE_64x64W = 4,    // region 64 x 64, 1024 threads (single precision)
+  TILE_128x32W = 5,   // region 128 x 32, 1024 threads (single precision)
 };
 int tile_region_x(int shape);
 int tile_region_y(int shape);
