@@ -33,6 +33,7 @@ extern "C" {
 #define NLS_ERR_NOMEM 6       /* device memory exhausted */
 #define NLS_ERR_BUSY 7        /* serving pool: no slot or admission budget for this request now */
 #define NLS_ERR_NOT_READY 8   /* serving pool: nothing finished yet */
+#define NLS_ERR_TOO_LARGE 9   /* nls_solve_2d_noalloc: grid beyond NLS_NOALLOC_MAX_NODES */
 
 /* ---- precisions -------------------------------------------------------------------------- */
 #define NLS_C128 0            /* complex128 state, float64 pump: the plain (drop-in) path */
@@ -154,6 +155,27 @@ int nls_pool_take(nls_pool* pool, int64_t* tag, void* u, size_t u_bytes);
 int nls_pool_status(nls_pool* pool, int* active, size_t* bytes_in_use);
 int nls_pool_destroy(nls_pool* pool);
 
+/* ---- allocation-free 2-D solve ------------------------------------------------------------ */
+/* No counterpart in the reference: the reference allocates its work arrays on every call.
+ *
+ * For callers that must not allocate device memory: services that reserve their whole device
+ * budget at start-up and may never grow it, host frameworks whose own caching allocator owns the
+ * GPU's memory, and latency-critical loops that cannot pay for cudaMalloc / cudaFree, which can
+ * synchronise the device and stall unrelated streams.  The call advances u_dev (n x n, in place)
+ * by iters RK4 steps of the 2-D model with the same fused tile kernel as nls_solve_device, on the
+ * caller's stream (NULL = the legacy default stream), with no cudaMalloc, cudaFree or other
+ * allocating call: its scratch (the second state buffer, the descriptor and the tile list) is a
+ * fixed file-scope device array of about 4 MiB, which every GPU that loads this library holds
+ * until the process exits.  Limits: dim must be 2 and n * n <= NLS_NOALLOC_MAX_NODES (512 x 512),
+ * otherwise NLS_ERR_TOO_LARGE.  The first call on a device resolves the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ * capture.  Every call shares the one array and it keeps the last call's contents (nothing in it
+ * needs to start at zero: the first step overwrites every node it later reads), so calls that
+ * overlap on the GPU -- on different streams or threads -- race; serialise them.  Returns after
+ * enqueueing the work (no host synchronisation). */
+#define NLS_NOALLOC_MAX_NODES 262144
+int nls_solve_2d_noalloc(int dtype, const nls_problem* problem, int64_t iters,
+                         const void* pumping_dev, void* u_dev, void* stream);
 
 #ifdef __cplusplus
 }

@@ -24,6 +24,8 @@ NLS_ERR_TIMEOUT = 5
 NLS_ERR_NOMEM = 6
 NLS_ERR_BUSY = 7
 NLS_ERR_NOT_READY = 8
+NLS_ERR_TOO_LARGE = 9
+NLS_NOALLOC_MAX_NODES = 262144
 
 NLS_C128 = 0
 NLS_C64 = 1
@@ -37,6 +39,7 @@ _STATUS_NAMES = {
     NLS_ERR_NOMEM: "out of device memory",
     NLS_ERR_BUSY: "busy",
     NLS_ERR_NOT_READY: "not ready",
+    NLS_ERR_TOO_LARGE: "grid too large for the allocation-free entry point",
 }
 
 # Every symbol include/nls_gb300.h declares, with (restype, argtypes).
@@ -84,6 +87,7 @@ SIGNATURES = {
     "nls_pool_take": (_i, [_p, _pi64, _p, _sz]),
     "nls_pool_status": (_i, [_p, _pi, _psz]),
     "nls_pool_destroy": (_i, [_p]),
+    "nls_solve_2d_noalloc": (_i, [_i, _pp, _i64, _p, _p, _p]),
 }
 
 _lib = None

@@ -22,7 +22,7 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libnls_gb300.so")
 
-SOURCES = ["k1d.cu", "k2d.cu", "kdiag.cu", "runtime.cu", "host_ops.cpp"]
+SOURCES = ["k1d.cu", "k2d.cu", "kdiag.cu", "runtime.cu", "noalloc.cu", "host_ops.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]

@@ -1,0 +1,125 @@
+// noalloc.cu -- an allocation-free entry point for the 2-D fused RK4 step.
+//
+// nls_solve_device() keeps a per-context scratch state buffer, descriptor and tile list that it
+// obtains with cudaMalloc on first use.  Some callers cannot allow that: a service that reserves
+// all of its device memory up front and must never grow it, a host framework whose own caching
+// allocator owns the GPU's memory, or a latency-critical loop that cannot afford cudaMalloc /
+// cudaFree, which may synchronise the whole device and stall unrelated streams.
+// nls_solve_2d_noalloc() serves them: it runs the same fused tile kernel (rk4_2d_fused), but its
+// scratch -- the second state buffer of the ping-pong, the instance descriptor and the tile list
+// -- lives in one file-scope __device__ array of fixed size, so the call allocates nothing.
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/nls_gb300.h"
+#include "kernels.h"
+#include "nls_types.h"
+
+#define NLS_API extern "C" __attribute__((visibility("default")))
+
+namespace nlsg {
+int host_stencil_2d(int order, double h, Stencil2D* s);
+}
+using namespace nlsg;
+
+namespace {
+
+constexpr size_t kStateBytes = (size_t)NLS_NOALLOC_MAX_NODES * 16;  // complex128 worst case
+constexpr size_t kDescBytes = 256;                                   // one Inst2D, padded
+constexpr size_t kMaxTiles = 16384;                                  // >= tiles of any allowed grid
+constexpr size_t kTileBytes = kMaxTiles * sizeof(TileItem);
+constexpr size_t kScratchBytes = kStateBytes + kDescBytes + kTileBytes;
+
+// Every GPU that loads the library holds this array until the process exits.  All calls share
+// it and it keeps whatever the last call left there.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+static_assert(sizeof(Inst2D) <= kDescBytes, "descriptor slot too small");
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void* g_scratch_dev[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device; resolved once per device.
+cudaError_t scratch_address(int device, char** out) {
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_scratch_dev[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    if (!p) return cudaErrorInvalidSymbol;
+    g_scratch_dev[device] = p;
+  }
+  *out = (char*)g_scratch_dev[device];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+NLS_API int nls_solve_2d_noalloc(int dtype, const nls_problem* pr, int64_t iters, const void* pumping_dev,
+                                 void* u_dev, void* stream) {
+  if (!pr || !pumping_dev || !u_dev || iters < 0) return NLS_ERR_INVALID;
+  if (dtype != NLS_C128 && dtype != NLS_C64) return NLS_ERR_INVALID;
+  if (pr->dim != 2) return NLS_ERR_INVALID;
+  if (pr->order != 3 && pr->order != 5) return NLS_ERR_ORDER;
+  if (pr->n < pr->order || !(pr->dx > 0.0)) return NLS_ERR_INVALID;
+  if ((int64_t)pr->n * pr->n > (int64_t)NLS_NOALLOC_MAX_NODES) return NLS_ERR_TOO_LARGE;
+  Stencil2D op;
+  if (host_stencil_2d(pr->order, pr->dx, &op)) return NLS_ERR_ORDER;
+  // fused tile shape: the caller's choice if it names a fused tile this precision supports,
+  // otherwise 64x64 (complex64) or 32x32 (complex128)
+  int shape = dtype == NLS_C64 ? TILE_64x64 : TILE_32x32;
+  if (pr->variant > 0 && tile_supported(pr->variant, dtype)) shape = pr->variant;
+  const int n = pr->n;
+  const int tx = tile_out_x(shape, op.K), ty = tile_out_y(shape, op.K);
+  const int tiles_x = (n + tx - 1) / tx;
+  const int n_items = tiles_x * ((n + ty - 1) / ty);
+  if ((size_t)n_items > kMaxTiles) return NLS_ERR_TOO_LARGE;
+  if (iters == 0) return NLS_OK;
+
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return NLS_ERR_CUDA;
+  char* base = nullptr;
+  if (scratch_address(device, &base) != cudaSuccess) return NLS_ERR_CUDA;
+  void* state2 = base;
+  Inst2D* dI = (Inst2D*)(base + kStateBytes);
+  TileItem* dT = (TileItem*)(base + kStateBytes + kDescBytes);
+  cudaStream_t st = (cudaStream_t)stream;
+
+  Inst2D I;
+  std::memset(&I, 0, sizeof(I));
+  I.u[0] = u_dev;
+  I.u[1] = state2;
+  I.P = pumping_dev;
+  I.n = n;
+  I.tiles_x = tiles_x;
+  I.parity = 0;
+  I.steps = INT64_MAX;
+  I.dt = pr->dt;
+  I.ph.c3 = pr->coeffs[2]; I.ph.c4 = pr->coeffs[3]; I.ph.c5 = pr->coeffs[4]; I.ph.c6 = pr->coeffs[5];
+  I.ph.c12 = pr->coeffs[11]; I.ph.c13 = pr->coeffs[12]; I.ph.c14 = pr->coeffs[13];
+  I.op = op;
+  std::vector<TileItem> items(n_items);
+  for (int t = 0; t < n_items; ++t) items[t] = TileItem{0, t};
+  // Pageable host sources: each copy returns once its bytes are staged, so the host vectors
+  // may go out of scope afterwards; the kernels below are ordered after the copies on `st`.
+  if (cudaMemcpyAsync(dI, &I, sizeof(I), cudaMemcpyHostToDevice, st) != cudaSuccess) return NLS_ERR_CUDA;
+  if (cudaMemcpyAsync(dT, items.data(), sizeof(TileItem) * n_items, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return NLS_ERR_CUDA;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return NLS_ERR_CUDA;
+  const int occ = fused_2d_blocks_per_sm(dtype, op.K, shape);
+  const int grid = n_items < sms * (occ > 0 ? occ : 1) ? n_items : sms * (occ > 0 ? occ : 1);
+  for (int64_t j = 0; j < iters; ++j) {
+    if (launch_2d_fused(dtype, op.K, shape, dI, dT, n_items, (int)(j & 1), grid, st) != cudaSuccess)
+      return NLS_ERR_CUDA;
+  }
+  // After an odd number of steps the state sits in the scratch buffer: bring it home.
+  if (iters & 1) {
+    const size_t bytes = (size_t)n * n * (dtype == NLS_C128 ? 16 : 8);
+    if (cudaMemcpyAsync(u_dev, state2, bytes, cudaMemcpyDeviceToDevice, st) != cudaSuccess) return NLS_ERR_CUDA;
+  }
+  return NLS_OK;
+}
