@@ -247,6 +247,32 @@ def run_grid(args):
     return 0
 
 
+def run_precision(args):
+    """--workload precision2d: 1024^2 on [-40, 40]^2, ring radius 15 width 2, order 5, dt 1e-5,
+    50 000 complex64 steps with FP64 norm / chemical potential every 500 steps, then the relative
+    L2 error of |psi|^2 and n against a complex128 run of the same problem."""
+    import torch
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    from nls_gb300 import build as nbuild
+    nbuild.build()
+    from nls_gb300 import precision, workloads
+    s, steps = workloads.precision_2d()
+    if args.solve_steps != SOLVE_STEPS:
+        steps = args.solve_steps
+    res = precision.run(s, steps=steps, log_every=500, device=local)
+    log = res["log"]
+    print(json.dumps({
+        "workload": "precision2d: 1024x1024 on [-40,40]^2, ring radius 15 width 2 amplitude 6, order 5, dt 1e-5, "
+                    f"{steps} steps, complex64 state, FP64 diagnostics every 500 steps",
+        "c64_node_steps_per_s": res["c64_node_steps_per_s"], "c64_seconds": res["c64_seconds"],
+        "c128_node_steps_per_s": res["c128_node_steps_per_s"], "c128_seconds": res["c128_seconds"],
+        "rel_l2_density": res["rel_l2_density"], "rel_l2_reservoir": res["rel_l2_reservoir"],
+        "log_first": log[0], "log_last": log[-1], "log_entries": len(log),
+        "norm_min": min(e["norm"] for e in log), "norm_max": max(e["norm"] for e in log)}))
+    return 0
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_init()
@@ -424,7 +450,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
     ap.add_argument("--quick", action="store_true",
                     help="timed batched solves only (no roofline, accuracy, e2e, serve or CPU legs)")
-    ap.add_argument("--workload", choices=["batch", "grid1d", "grid2d"], default="batch")
+    ap.add_argument("--workload", choices=["batch", "grid1d", "grid2d", "precision2d"], default="batch")
     ap.add_argument("--solve-steps", type=int, default=SOLVE_STEPS, help="RK4 steps per solve")
     ap.add_argument("--n", type=int, default=4096, help="grid size for grid1d/grid2d")
     ap.add_argument("--order", type=int, default=3, help="stencil order for grid1d/grid2d")
@@ -433,6 +459,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "precision2d":
+        return run_precision(args)
     if args.workload != "batch":
         return run_grid(args)
     return run_ours(args)

@@ -107,6 +107,12 @@ int nls_chemical_potential_2d(nls_ctx* ctx, int dtype, double dx, int n, const d
                               const void* pumping, const void* u0, double* mu);
 
 /* ---- FP64 device diagnostics (no reference counterpart: the reference has none) ----------- */
+/* Chemical potential of a device-resident state, as chemical_potential_1d/2d (nls/nls.f90:921-971,
+ * order-5 operator, radial weight in 1-D) but on device pointers and in FP64: mu = mu_re + i mu_im
+ * (the 2-D reference returns mu_re only).  problem supplies dim, n, dx and coeffs.  Blocks. */
+int nls_chemical_potential_device(nls_ctx* ctx, int dtype, const nls_problem* problem,
+                                  const void* pumping_dev, const void* u_dev, double* mu_re,
+                                  double* mu_im);
 /* sum |u|^2 over count nodes and the number of non-finite components; blocks until done. */
 int nls_norm_device(nls_ctx* ctx, int dtype, int64_t count, const void* u_dev, double* sum_sq,
                     int64_t* nonfinite);

@@ -98,6 +98,11 @@ int host_stencil_1d(int n, int order, double h, Stencil1D* s) {
       const int q = p + i - s->K;
       s->near[p][i] = (q >= 0 && q < n) ? rows[(size_t)p * W + i] : 0.0;
     }
+  for (int i = 0; i < 7; ++i) {
+    s->w2f[i] = (float)s->w2[i];
+    s->w1f[i] = (float)s->w1[i];
+    for (int p = 0; p < 3; ++p) s->nearf[p][i] = (float)s->near[p][i];
+  }
   return 0;
 }
 

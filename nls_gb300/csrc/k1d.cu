@@ -30,8 +30,8 @@ __device__ __forceinline__ Weights1D<T, K> load_w(const Stencil1D& s) {
   Weights1D<T, K> w;
 #pragma unroll
   for (int i = 0; i < 2 * K + 1; ++i) {
-    w.w2[i] = (T)s.w2[i];
-    w.w1[i] = (T)s.w1[i];
+    w.w2[i] = ParamsOf<T>::w2(s, i);
+    w.w1[i] = ParamsOf<T>::w1(s, i);
   }
   return w;
 }
@@ -61,7 +61,7 @@ __device__ __forceinline__ typename C2<T>::type lap1d(const typename C2<T>::type
     T lx = 0, ly = 0;
 #pragma unroll
     for (int d = -K; d <= K; ++d) {
-      T a = (T)s.near[p][d + K];
+      T a = ParamsOf<T>::near(s, p, d + K);
       C v = in[c + d];
       lx += a * v.x;
       ly += a * v.y;
@@ -106,8 +106,9 @@ __global__ void __launch_bounds__(512) rk4_1d_resident(const Inst1D* __restrict_
   for (int i = tid; i < 2 * L; i += NT) buf[0][i] = mk<T>(0, 0);
   if (cl > 1) cluster.sync(); else __syncthreads();
 
-  const Phys<T> ph = phys_from<T>(I.ph);
-  const RK<T> rk = rk_from<T>(I.dt);
+  const Params<T>& prm = ParamsOf<T>::get(I);
+  const Phys<T> ph = phys_of<T>(prm);
+  const RK<T> rk = rk_of<T>(prm);
   const Weights1D<T, K> w = load_w<T, K>(I.op);
   const T h = (T)I.op.h;
   const C* __restrict__ Ug = reinterpret_cast<const C*>(I.u);
@@ -134,6 +135,14 @@ __global__ void __launch_bounds__(512) rk4_1d_resident(const Inst1D* __restrict_
   }
   if (cl > 1) cluster.sync(); else __syncthreads();
 
+  // the pump enters as c12 * P (the reference evaluates coeffs(12) * pumping first)
+#pragma unroll
+  for (int j = 0; j < NPT; ++j) P[j] = ph.c12 * P[j];
+  // Nodes are processed in batches of CB: a batch's shared-memory loads are all issued before any
+  // of its stores and its arithmetic is written phase by phase across the batch, so the nodes'
+  // independent dependency chains overlap.
+  constexpr int CB0 = (sizeof(T) == 8 || K == 3) ? 2 : 4;
+  constexpr int CB = NPT < CB0 ? NPT : CB0;
   const int64_t steps = I.steps;
   for (int64_t step = 0; step < steps; ++step) {
 #pragma unroll 1
@@ -141,39 +150,80 @@ __global__ void __launch_bounds__(512) rk4_1d_resident(const Inst1D* __restrict_
       const C* in = buf[(s & 1) ? 0 : 1];
       const int ob = (s & 1) ? 1 : 0;
       C* out = buf[ob];
+      const T coef = s == 3 ? rk.dt : rk.half_dt;
+      const T wk = (s == 2 || s == 3) ? (T)2 : (T)1;
 #pragma unroll
-      for (int j = 0; j < NPT; ++j) {
-        const int li = tid + j * NT;
-        if (li < len) {
-          const int p = p0 + li;
-          const int c = K + li;
-          const C lu = lap1d<T, K>(in, c, p, ir[j], w, I.op);
-          const C k = rhs<T>(in[c], P[j], lu, ph);
-          C t;
-          if (s == 1) {
-            acc[j] = k;
-            t.x = u[j].x + rk.half_dt * k.x;
-            t.y = u[j].y + rk.half_dt * k.y;
-          } else if (s == 2) {
-            acc[j].x += (T)2 * k.x;
-            acc[j].y += (T)2 * k.y;
-            t.x = u[j].x + rk.half_dt * k.x;
-            t.y = u[j].y + rk.half_dt * k.y;
-          } else if (s == 3) {
-            acc[j].x += (T)2 * k.x;
-            acc[j].y += (T)2 * k.y;
-            t.x = u[j].x + rk.dt * k.x;
-            t.y = u[j].y + rk.dt * k.y;
+      for (int j0 = 0; j0 < NPT; j0 += CB) {
+        C v[CB][2 * K + 1];
+#pragma unroll
+        for (int i = 0; i < CB; ++i) {
+          const int li = tid + (j0 + i) * NT;
+          const int c = K + (li < len ? li : 0);
+#pragma unroll
+          for (int d = -K; d <= K; ++d) v[i][d + K] = in[c + d];
+        }
+        C lu[CB];
+#pragma unroll
+        for (int i = 0; i < CB; ++i) {
+          const int p = p0 + tid + (j0 + i) * NT;
+          if (p >= K) {
+            T d2x = 0, d2y = 0, d1x = 0, d1y = 0;
+#pragma unroll
+            for (int d = -K; d <= K; ++d) {
+              d2x += w.w2[d + K] * v[i][d + K].x;
+              d2y += w.w2[d + K] * v[i][d + K].y;
+              if (d != 0) {
+                d1x += w.w1[d + K] * v[i][d + K].x;
+                d1y += w.w1[d + K] * v[i][d + K].y;
+              }
+            }
+            lu[i].x = d2x + ir[j0 + i] * d1x;
+            lu[i].y = d2y + ir[j0 + i] * d1y;
           } else {
-            acc[j].x += k.x;
-            acc[j].y += k.y;
+            T lx = 0, ly = 0;
+#pragma unroll
+            for (int d = -K; d <= K; ++d) {
+              const T a = ParamsOf<T>::near(I.op, p, d + K);
+              lx += a * v[i][d + K].x;
+              ly += a * v[i][d + K].y;
+            }
+            lu[i].x = lx;
+            lu[i].y = ly;
+          }
+        }
+        T sq[CB], r[CB];
+#pragma unroll
+        for (int i = 0; i < CB; ++i) sq[i] = v[i][K].x * v[i][K].x + v[i][K].y * v[i][K].y;
+#pragma unroll
+        for (int i = 0; i < CB; ++i) r[i] = rdiv(P[j0 + i], ph.c13 + ph.c14 * sq[i]);
+#pragma unroll
+        for (int i = 0; i < CB; ++i) {
+          const int j = j0 + i;
+          const int li = tid + j * NT;
+          const T a = ph.c3 * r[i] - ph.c4;
+          const T b = ph.c5 * sq[i] + ph.c6 * r[i];
+          C k;
+          k.x = a * v[i][K].x + b * v[i][K].y - lu[i].y;
+          k.y = a * v[i][K].y - b * v[i][K].x + lu[i].x;
+          if (s == 1) acc[j] = k;
+          else {
+            acc[j].x += wk * k.x;
+            acc[j].y += wk * k.y;
+          }
+          C t;
+          if (s < 4) {
+            t.x = u[j].x + coef * k.x;
+            t.y = u[j].y + coef * k.y;
+          } else {
             u[j].x = u[j].x + rk.dt6 * acc[j].x;
             u[j].y = u[j].y + rk.dt6 * acc[j].y;
             t = u[j];
           }
-          out[c] = t;
-          if (left_buf[ob] && li < K) left_buf[ob][seg + K + li] = t;
-          if (right_buf[ob] && li >= seg - K) right_buf[ob][li - (seg - K)] = t;
+          if (li < len) {
+            out[K + li] = t;
+            if (left_buf[ob] && li < K) left_buf[ob][seg + K + li] = t;
+            if (right_buf[ob] && li >= seg - K) right_buf[ob][li - (seg - K)] = t;
+          }
         }
       }
       if (cl > 1) cluster.sync(); else __syncthreads();
@@ -194,7 +244,7 @@ template <typename T, int K>
 __global__ void __launch_bounds__(256) rk4_1d_stage(int n, int s, const void* __restrict__ src_,
                                                     void* __restrict__ u_, const void* __restrict__ P_,
                                                     void* __restrict__ acc_, void* __restrict__ dst_,
-                                                    double dt, PhysD phd, Stencil1D op) {
+                                                    Params<T> prm, Stencil1D op, T h) {
   typedef typename C2<T>::type C;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
@@ -203,8 +253,8 @@ __global__ void __launch_bounds__(256) rk4_1d_stage(int n, int s, const void* __
   const T* __restrict__ P = reinterpret_cast<const T*>(P_);
   C* __restrict__ acc = reinterpret_cast<C*>(acc_);
   C* __restrict__ dst = reinterpret_cast<C*>(dst_);
-  const Phys<T> ph = phys_from<T>(phd);
-  const RK<T> rk = rk_from<T>(dt);
+  const Phys<T> ph = phys_of<T>(prm);
+  const RK<T> rk = rk_of<T>(prm);
   const Weights1D<T, K> w = load_w<T, K>(op);
   // gather the 2K+1 neighbours with zero outside [0, n)
   C v[2 * K + 1];
@@ -213,7 +263,7 @@ __global__ void __launch_bounds__(256) rk4_1d_stage(int n, int s, const void* __
     const int q = p + d;
     v[d + K] = (q >= 0 && q < n) ? src[q] : mk<T>(0, 0);
   }
-  const T ir = p >= K ? (T)1 / ((T)p * (T)op.h) : (T)0;
+  const T ir = p >= K ? (T)1 / ((T)p * h) : (T)0;
   const C lu = lap1d<T, K>(v, K, p, ir, w, op);
   const C k = rhs<T>(v[K], P[p], lu, ph);
   const C u = U[p];
@@ -238,13 +288,13 @@ __global__ void __launch_bounds__(256) rk4_1d_stage(int n, int s, const void* __
 // v = H(u) for the diagnostics (chemical potential).
 template <typename T, int K>
 __global__ void __launch_bounds__(256) rhs_1d(int n, const void* __restrict__ u_, const void* __restrict__ P_,
-                                              void* __restrict__ v_, PhysD phd, Stencil1D op) {
+                                              void* __restrict__ v_, Params<T> prm, Stencil1D op, T h) {
   typedef typename C2<T>::type C;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   const C* __restrict__ u = reinterpret_cast<const C*>(u_);
   const T* __restrict__ P = reinterpret_cast<const T*>(P_);
-  const Phys<T> ph = phys_from<T>(phd);
+  const Phys<T> ph = phys_of<T>(prm);
   const Weights1D<T, K> w = load_w<T, K>(op);
   C v[2 * K + 1];
 #pragma unroll
@@ -252,7 +302,7 @@ __global__ void __launch_bounds__(256) rhs_1d(int n, const void* __restrict__ u_
     const int q = p + d;
     v[d + K] = (q >= 0 && q < n) ? u[q] : mk<T>(0, 0);
   }
-  const T ir = p >= K ? (T)1 / ((T)p * (T)op.h) : (T)0;
+  const T ir = p >= K ? (T)1 / ((T)p * h) : (T)0;
   reinterpret_cast<C*>(v_)[p] = rhs<T>(v[K], P[p], lap1d<T, K>(v, K, p, ir, w, op), ph);
 }
 
@@ -344,7 +394,14 @@ cudaError_t launch_1d_resident(int dtype, int K, const Inst1D* d_insts, int coun
 template <typename T, int K>
 static void stage_1d_t(int n, int s, const void* src, void* u, const void* P, void* acc, void* dst,
                        double dt, const PhysD& ph, const Stencil1D& op, cudaStream_t st) {
-  rk4_1d_stage<T, K><<<(n + 255) / 256, 256, 0, st>>>(n, s, src, u, P, acc, dst, dt, ph, op);
+  rk4_1d_stage<T, K><<<(n + 255) / 256, 256, 0, st>>>(n, s, src, u, P, acc, dst,
+                                                      make_params<T>(ph, dt, 0.0, 0.0, 0.0), op, (T)op.h);
+}
+
+template <typename T, int K>
+static void rhs_1d_t(int n, const void* u, const void* P, void* v, const PhysD& ph, const Stencil1D& op,
+                     cudaStream_t st) {
+  rhs_1d<T, K><<<(n + 255) / 256, 256, 0, st>>>(n, u, P, v, make_params<T>(ph, 0.0, 0.0, 0.0, 0.0), op, (T)op.h);
 }
 
 cudaError_t launch_1d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,
@@ -368,16 +425,15 @@ cudaError_t launch_1d_stage(int dtype, int n, int s, const void* src, void* u, c
 cudaError_t launch_rhs_1d(int dtype, int n, const void* u, const void* P, void* v, const PhysD& ph,
                           const Stencil1D& op, cudaStream_t st) {
   const int K = op.K;
-  const int g = (n + 255) / 256;
   if (dtype == NLS_C128) {
-    if (K == 1) rhs_1d<double, 1><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
-    else if (K == 2) rhs_1d<double, 2><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
-    else if (K == 3) rhs_1d<double, 3><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
+    if (K == 1) rhs_1d_t<double, 1>(n, u, P, v, ph, op, st);
+    else if (K == 2) rhs_1d_t<double, 2>(n, u, P, v, ph, op, st);
+    else if (K == 3) rhs_1d_t<double, 3>(n, u, P, v, ph, op, st);
     else return cudaErrorInvalidValue;
   } else {
-    if (K == 1) rhs_1d<float, 1><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
-    else if (K == 2) rhs_1d<float, 2><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
-    else if (K == 3) rhs_1d<float, 3><<<g, 256, 0, st>>>(n, u, P, v, ph, op);
+    if (K == 1) rhs_1d_t<float, 1>(n, u, P, v, ph, op, st);
+    else if (K == 2) rhs_1d_t<float, 2>(n, u, P, v, ph, op, st);
+    else if (K == 3) rhs_1d_t<float, 3>(n, u, P, v, ph, op, st);
     else return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -11,6 +11,12 @@
 //
 // rk4_2d_stage: one RK4 stage from global memory (no halo recomputation), used where tiles would
 // be too small to amortise their halo (double precision on modest grids) and as the general path.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstring>
+#include <mutex>
+
 #include "kernels.h"
 #include "nls_common.cuh"
 
@@ -29,22 +35,27 @@ __device__ __forceinline__ float2 pfma(float s, float2 b, float2 c) { return __f
 __device__ __forceinline__ float2 pmul(float s, float2 b) { return __fmul2_rn(make_float2(s, s), b); }
 __device__ __forceinline__ double2 padd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 pfma(double s, double2 b, double2 c) {
-  return make_double2(fma(s, b.x, c.x), fma(s, b.y, c.y));
+  return make_double2(__fma_rn(s, b.x, c.x), __fma_rn(s, b.y, c.y));
 }
 __device__ __forceinline__ double2 pmul(double s, double2 b) { return make_double2(s * b.x, s * b.y); }
+
+// Fused multiply-add in the working precision (single-precision arguments must not be promoted
+// to the FP64 pipe, which runs at a small fraction of the FP32 rate on GB300).
+__device__ __forceinline__ float mad(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double mad(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 // Right-hand side with the pump already multiplied by c12 (the reference evaluates
 // coeffs(12) * pumping first, nls/nls.f90:580, so folding it changes no rounding).
 template <typename T>
 __device__ __forceinline__ typename C2<T>::type rhs_pc(typename C2<T>::type u, T pc,
                                                        typename C2<T>::type lu, const Phys<T>& ph) {
-  const T s = fma(u.x, u.x, u.y * u.y);
-  const T r = rdiv(pc, fma(ph.c14, s, ph.c13));
-  const T a = fma(ph.c3, r, -ph.c4);
-  const T b = fma(ph.c5, s, ph.c6 * r);
+  const T s = mad(u.x, u.x, u.y * u.y);
+  const T r = rdiv(pc, mad(ph.c14, s, ph.c13));
+  const T a = mad(ph.c3, r, -ph.c4);
+  const T b = mad(ph.c5, s, ph.c6 * r);
   typename C2<T>::type v;
-  v.x = fma(a, u.x, fma(b, u.y, -lu.y));
-  v.y = fma(a, u.y, fma(-b, u.x, lu.x));
+  v.x = mad(a, u.x, mad(b, u.y, -lu.y));
+  v.y = mad(a, u.y, mad(-b, u.x, lu.x));
   return v;
 }
 
@@ -63,59 +74,137 @@ struct TileCfg {
   static constexpr size_t SMEM = (size_t)2 * ROWS * RX * sizeof(typename C2<T>::type);
   // CTAs per SM the register budget is sized for: 2 x 256 threads, else one CTA
   static constexpr int MINB = NT <= 256 ? 2 : 1;
+  // rows per shared-memory load batch in a stage, sized to the register budget
+  static constexpr int CJ = (NT >= 1024 || sizeof(T) == 8) ? 2 : (NJ < 4 ? NJ : 4);
   static_assert(RX % 32 == 0 && RY % NS == 0 && NJ <= 32, "tile layout");
   static_assert(TX > 0 && TY > 0, "tile too small for its halo");
 };
 
 // One RK4 stage S over the thread's column strip.  Every node of the region is evaluated (the
 // stage's valid region shrinks by K per stage; values computed outside it are never read again),
-// and only in-domain nodes are stored, so out-of-domain halo stays exactly zero.
-template <typename T, int K, int RX, int NJ, int S>
+// and only in-domain nodes are stored, so out-of-domain halo stays exactly zero.  Rows are taken
+// in batches of CJ: all shared-memory loads of a batch are issued before any of its stores, so
+// the independent rows overlap their load and arithmetic latencies.
+template <typename T, int K, int RX, int NJ, int S, int CJ>
 __device__ __forceinline__ void tile_stage(const typename C2<T>::type* __restrict__ in,
                                            typename C2<T>::type* __restrict__ out, int x, int y0,
                                            typename C2<T>::type (&u)[NJ], typename C2<T>::type (&acc)[NJ],
                                            const T (&pc)[NJ], unsigned dom, const Phys<T>& ph,
                                            const RK<T>& rk, T wc, T w1, T w2) {
   typedef typename C2<T>::type C;
-  C w[2 * K + 1];
+  static_assert(NJ % CJ == 0, "row batches");
 #pragma unroll
-  for (int d = 0; d <= 2 * K; ++d) w[d] = in[(y0 - K + d) * RX + x];
+  for (int j0 = 0; j0 < NJ; j0 += CJ) {
+    C cv[CJ + 2 * K];
+    C hl[K][CJ], hr[K][CJ];
 #pragma unroll
-  for (int j = 0; j < NJ; ++j) {
-    const int c = (y0 + j) * RX + x;
-    const C v = w[K];
-    C s1 = padd(padd(in[c - 1], in[c + 1]), padd(w[K - 1], w[K + 1]));
-    C lu = pfma(w1, s1, pmul(wc, v));
-    if (K == 2) {
-      C s2 = padd(padd(in[c - 2], in[c + 2]), padd(w[0], w[2 * K]));
-      lu = pfma(w2, s2, lu);
+    for (int i = 0; i < CJ + 2 * K; ++i) cv[i] = in[(y0 + j0 - K + i) * RX + x];
+#pragma unroll
+    for (int d = 1; d <= K; ++d)
+#pragma unroll
+      for (int i = 0; i < CJ; ++i) {
+        hl[d - 1][i] = in[(y0 + j0 + i) * RX + x - d];
+        hr[d - 1][i] = in[(y0 + j0 + i) * RX + x + d];
+      }
+    // The arithmetic below is written phase by phase across the CJ rows of the batch, so the
+    // rows' independent dependency chains are interleaved in the instruction stream.
+    C lu[CJ];
+#pragma unroll
+    for (int i = 0; i < CJ; ++i) {
+      const C s1 = padd(padd(hl[0][i], hr[0][i]), padd(cv[i + K - 1], cv[i + K + 1]));
+      lu[i] = pfma(w1, s1, pmul(wc, cv[i + K]));
+      if (K == 2) {
+        const C s2 = padd(padd(hl[K - 1][i], hr[K - 1][i]), padd(cv[i], cv[i + 2 * K]));
+        lu[i] = pfma(w2, s2, lu[i]);
+      }
     }
-    const C k = rhs_pc<T>(v, pc[j], lu, ph);
-    if (S == 1) acc[j] = k;
-    else acc[j] = pfma(S == 4 ? (T)1 : (T)2, k, acc[j]);
-    if (S < 4) {
-      const C t = pfma(S == 3 ? rk.dt : rk.half_dt, k, u[j]);
-      if (dom & (1u << j)) out[c] = t;
-    } else {
-      u[j] = pfma(rk.dt6, acc[j], u[j]);
+    T sq[CJ], r[CJ];
+#pragma unroll
+    for (int i = 0; i < CJ; ++i) sq[i] = mad(cv[i + K].x, cv[i + K].x, cv[i + K].y * cv[i + K].y);
+#pragma unroll
+    for (int i = 0; i < CJ; ++i) r[i] = rdiv(pc[j0 + i], mad(ph.c14, sq[i], ph.c13));
+    C k[CJ];
+#pragma unroll
+    for (int i = 0; i < CJ; ++i) {
+      const T a = mad(ph.c3, r[i], -ph.c4);
+      const T b = mad(ph.c5, sq[i], ph.c6 * r[i]);
+      const C v = cv[i + K];
+      k[i].x = mad(a, v.x, mad(b, v.y, -lu[i].y));
+      k[i].y = mad(a, v.y, mad(-b, v.x, lu[i].x));
     }
 #pragma unroll
-    for (int d = 0; d < 2 * K; ++d) w[d] = w[d + 1];
-    if (j + 1 < NJ) w[2 * K] = in[(y0 + j + 1 + K) * RX + x];
+    for (int i = 0; i < CJ; ++i) {
+      const int j = j0 + i;
+      if (S == 1) acc[j] = k[i];
+      else acc[j] = pfma(S == 4 ? (T)1 : (T)2, k[i], acc[j]);
+      if (S < 4) {
+        const C t = pfma(S == 3 ? rk.dt : rk.half_dt, k[i], u[j]);
+        if (dom & (1u << j)) out[(y0 + j) * RX + x] = t;
+      } else {
+        u[j] = pfma(rk.dt6, acc[j], u[j]);
+      }
+    }
   }
 }
 
-template <typename T, int K, int RX, int RY, int NS>
+// ---- TMA / mbarrier helpers (inline PTX, sm_90+ forms valid on sm_103a)
+
+// Set when a bounded wait on a tile copy gives up; read and cleared by the host.
+__device__ int g_tile_wait_timeout = 0;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// 2-D tiled TMA load of the box at (x, y) (x = innermost coordinate) into shared memory.
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+// Bounded wait for phase `parity` of the barrier: at most kWaitIters polls with a 1 us suspend
+// hint each (about a second); returns false if the phase never completed.
+constexpr int kWaitIters = 1 << 20;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (int i = 0; i < kWaitIters; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done) : "r"(a), "r"(parity), "r"(1000) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+template <typename T, int K, int RX, int RY, int NS, bool TMA>
 __global__ void __launch_bounds__(TileCfg<T, K, RX, RY, NS>::NT, TileCfg<T, K, RX, RY, NS>::MINB)
 rk4_2d_fused(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items, int n_items,
              int j_step) {
   typedef typename C2<T>::type C;
   typedef TileCfg<T, K, RX, RY, NS> G;
   constexpr int NJ = G::NJ, H = G::H;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   C* base = reinterpret_cast<C*>(smem_raw);
   C* buf0 = base + K * RX;                   // row 0 of buffer 0 (rows -K .. RY+K-1 exist)
   C* buf1 = base + G::ROWS * RX + K * RX;
+  // TMA path only: staging for the next tile's state and pump boxes, and their barrier
+  C* stage_u = reinterpret_cast<C*>(smem_raw + G::SMEM);
+  T* stage_p = reinterpret_cast<T*>(smem_raw + G::SMEM + (size_t)RX * RY * sizeof(C));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + G::SMEM + (size_t)RX * RY * (sizeof(C) + sizeof(T)));
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int x = (warp % G::WX) * 32 + lane;
   const int y0 = (warp / G::WX) * NJ;
@@ -128,10 +217,44 @@ rk4_2d_fused(const Inst2D* __restrict__ insts, const TileItem* __restrict__ item
   }
   const bool x_interior = x >= H && x < RX - H;
 
-  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+  auto active = [&](int idx) -> bool {
+    return idx < n_items && (int64_t)j_step < insts[items[idx].inst].steps;
+  };
+  // thread 0 arms the barrier and issues the state and pump boxes of tile idx
+  auto issue = [&](int idx) {
+    const TileItem ti = items[idx];
+    const Inst2D& I = insts[ti.inst];
+    const int tyi = ti.tile / I.tiles_x;
+    const int txi = ti.tile - tyi * I.tiles_x;
+    const int par = (I.parity + j_step) & 1;
+    const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(I.tmap);
+    fence_proxy_async_smem();
+    mbar_expect_tx(bar, (uint32_t)((size_t)RX * RY * (sizeof(C) + sizeof(T))));
+    tma_load_2d(stage_u, maps + par, txi * G::TX - H, tyi * G::TY - H, bar);
+    tma_load_2d(stage_p, maps + 2, txi * G::TX - H, tyi * G::TY - H, bar);
+  };
+  uint32_t phase = 0;
+  int it = blockIdx.x;
+  if (TMA) {
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    while (it < n_items && !active(it)) it += gridDim.x;
+    if (threadIdx.x == 0 && it < n_items) issue(it);
+  }
+
+  while (it < n_items) {
     const TileItem ti = items[it];
     const Inst2D& I = insts[ti.inst];
-    if ((int64_t)j_step >= I.steps) continue;
+    int nxt = it + gridDim.x;
+    if (TMA) {
+      while (nxt < n_items && !active(nxt)) nxt += gridDim.x;
+    } else if ((int64_t)j_step >= I.steps) {
+      it = nxt;
+      continue;
+    }
     const int n = I.n;
     const int par = (I.parity + j_step) & 1;
     const C* __restrict__ src = reinterpret_cast<const C*>(I.u[par]);
@@ -142,21 +265,41 @@ rk4_2d_fused(const Inst2D* __restrict__ insts, const TileItem* __restrict__ item
     const int gx = txi * G::TX - H + x;
     const int gy0 = tyi * G::TY - H + y0;
     const bool xin = gx >= 0 && gx < n;
-    const Phys<T> ph = phys_from<T>(I.ph);
-    const RK<T> rk = rk_from<T>(I.dt);
-    const T wc = (T)I.op.center, w1 = (T)I.op.w[0], w2 = (T)I.op.w[1];
-    const T c12 = (T)I.ph.c12;
+    const Params<T>& prm = ParamsOf<T>::get(I);
+    const Phys<T> ph = phys_of<T>(prm);
+    const RK<T> rk = rk_of<T>(prm);
+    const T wc = prm.wc, w1 = prm.w1, w2 = prm.w2;
+    const T c12 = prm.c12;
 
     C u[NJ], acc[NJ];
     T pc[NJ];
     unsigned dom = 0, store = 0;
+    if (TMA) {
+      // one bounded wait per tile; a timeout ends every thread of the CTA together
+      bool ok = true;
+      if (threadIdx.x == 0) ok = mbar_wait(bar, phase);
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+          atomicExch(&g_tile_wait_timeout, 1);
+          mbar_wait(bar, phase);   // let the copy in flight land before the CTA leaves
+        }
+        return;
+      }
+      phase ^= 1u;
+    }
 #pragma unroll
     for (int j = 0; j < NJ; ++j) {
       const int gy = gy0 + j;
       const bool inb = xin && gy >= 0 && gy < n;
-      const size_t q = (size_t)gy * n + gx;
-      u[j] = inb ? src[q] : mk<T>(0, 0);
-      pc[j] = inb ? c12 * Pg[q] : (T)0;
+      if (TMA) {
+        // out-of-range parts of the box arrive zero-filled
+        u[j] = stage_u[(y0 + j) * RX + x];
+        pc[j] = c12 * stage_p[(y0 + j) * RX + x];
+      } else {
+        const size_t q = (size_t)gy * n + gx;
+        u[j] = inb ? src[q] : mk<T>(0, 0);
+        pc[j] = inb ? c12 * Pg[q] : (T)0;
+      }
       acc[j] = mk<T>(0, 0);
       dom |= (unsigned)inb << j;
       const int y = y0 + j;
@@ -168,17 +311,20 @@ rk4_2d_fused(const Inst2D* __restrict__ insts, const TileItem* __restrict__ item
       if (!(dom & (1u << j))) buf1[(y0 + j) * RX + x] = mk<T>(0, 0);
     }
     __syncthreads();
-    tile_stage<T, K, RX, NJ, 1>(buf0, buf1, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
+    // the staging buffer is free again: fetch the next tile while this one is computed
+    if (TMA && threadIdx.x == 0 && nxt < n_items) issue(nxt);
+    tile_stage<T, K, RX, NJ, 1, G::CJ>(buf0, buf1, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
     __syncthreads();
-    tile_stage<T, K, RX, NJ, 2>(buf1, buf0, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
+    tile_stage<T, K, RX, NJ, 2, G::CJ>(buf1, buf0, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
     __syncthreads();
-    tile_stage<T, K, RX, NJ, 3>(buf0, buf1, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
+    tile_stage<T, K, RX, NJ, 3, G::CJ>(buf0, buf1, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
     __syncthreads();
-    tile_stage<T, K, RX, NJ, 4>(buf1, nullptr, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
+    tile_stage<T, K, RX, NJ, 4, G::CJ>(buf1, nullptr, x, y0, u, acc, pc, dom, ph, rk, wc, w1, w2);
 #pragma unroll
     for (int j = 0; j < NJ; ++j)
       if (store & (1u << j)) dst[(size_t)(gy0 + j) * n + gx] = u[j];
     __syncthreads();  // the next tile's load rewrites both buffers
+    it = nxt;
   }
 }
 
@@ -187,7 +333,7 @@ template <typename T, int K>
 __global__ void __launch_bounds__(256) rk4_2d_stage(int n, int s, const void* __restrict__ src_,
                                                     void* __restrict__ u_, const void* __restrict__ P_,
                                                     void* __restrict__ acc_, void* __restrict__ dst_,
-                                                    double dt, PhysD phd, Stencil2D op) {
+                                                    Params<T> prm) {
   typedef typename C2<T>::type C;
   const int x = blockIdx.x * 32 + (threadIdx.x & 31);
   const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -197,15 +343,15 @@ __global__ void __launch_bounds__(256) rk4_2d_stage(int n, int s, const void* __
   const T* __restrict__ P = reinterpret_cast<const T*>(P_);
   C* __restrict__ acc = reinterpret_cast<C*>(acc_);
   C* __restrict__ dst = reinterpret_cast<C*>(dst_);
-  const Phys<T> ph = phys_from<T>(phd);
-  const RK<T> rk = rk_from<T>(dt);
+  const Phys<T> ph = phys_of<T>(prm);
+  const RK<T> rk = rk_of<T>(prm);
   const size_t q = (size_t)y * n + x;
   auto at = [&](int xx, int yy) -> C {
     return (xx >= 0 && xx < n && yy >= 0 && yy < n) ? src[(size_t)yy * n + xx] : mk<T>(0, 0);
   };
   const C v = src[q];
   const C s1 = cadd4<T>(at(x - 1, y), at(x + 1, y), at(x, y - 1), at(x, y + 1));
-  const T wc = (T)op.center, w1 = (T)op.w[0], w2 = (T)op.w[1];
+  const T wc = prm.wc, w1 = prm.w1, w2 = prm.w2;
   C lu = mk<T>(wc * v.x + w1 * s1.x, wc * v.y + w1 * s1.y);
   if (K == 2) {
     const C s2 = cadd4<T>(at(x - 2, y), at(x + 2, y), at(x, y - 2), at(x, y + 2));
@@ -234,21 +380,21 @@ __global__ void __launch_bounds__(256) rk4_2d_stage(int n, int s, const void* __
 
 template <typename T, int K>
 __global__ void __launch_bounds__(256) rhs_2d(int n, const void* __restrict__ u_, const void* __restrict__ P_,
-                                              void* __restrict__ v_, PhysD phd, Stencil2D op) {
+                                              void* __restrict__ v_, Params<T> prm) {
   typedef typename C2<T>::type C;
   const int x = blockIdx.x * 32 + (threadIdx.x & 31);
   const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
   if (x >= n || y >= n) return;
   const C* __restrict__ src = reinterpret_cast<const C*>(u_);
   const T* __restrict__ P = reinterpret_cast<const T*>(P_);
-  const Phys<T> ph = phys_from<T>(phd);
+  const Phys<T> ph = phys_of<T>(prm);
   auto at = [&](int xx, int yy) -> C {
     return (xx >= 0 && xx < n && yy >= 0 && yy < n) ? src[(size_t)yy * n + xx] : mk<T>(0, 0);
   };
   const size_t q = (size_t)y * n + x;
   const C v = src[q];
   const C s1 = cadd4<T>(at(x - 1, y), at(x + 1, y), at(x, y - 1), at(x, y + 1));
-  const T wc = (T)op.center, w1 = (T)op.w[0], w2 = (T)op.w[1];
+  const T wc = prm.wc, w1 = prm.w1, w2 = prm.w2;
   C lu = mk<T>(wc * v.x + w1 * s1.x, wc * v.y + w1 * s1.y);
   if (K == 2) {
     const C s2 = cadd4<T>(at(x - 2, y), at(x + 2, y), at(x, y - 2), at(x, y + 2));
@@ -289,25 +435,42 @@ bool tile_supported(int shape, int dtype) {
   return false;
 }
 
-template <typename T, int K, int RX, int RY, int NS>
+template <typename T, int K, int RX, int RY, int NS, bool TMA>
+static size_t smem_f() {
+  typedef TileCfg<T, K, RX, RY, NS> G;
+  return TMA ? G::SMEM + (size_t)RX * RY * (sizeof(typename C2<T>::type) + sizeof(T)) + 128 : G::SMEM;
+}
+
+template <typename T, int K, int RX, int RY, int NS, bool TMA = false>
 static cudaError_t launch_f(const Inst2D* d_insts, const TileItem* d_items, int n_items, int j_step,
                             int grid, cudaStream_t s) {
   typedef TileCfg<T, K, RX, RY, NS> G;
-  auto kern = rk4_2d_fused<T, K, RX, RY, NS>;
-  kern<<<grid, G::NT, G::SMEM, s>>>(d_insts, d_items, n_items, j_step);
+  auto kern = rk4_2d_fused<T, K, RX, RY, NS, TMA>;
+  kern<<<grid, G::NT, smem_f<T, K, RX, RY, NS, TMA>(), s>>>(d_insts, d_items, n_items, j_step);
   return cudaGetLastError();
 }
 
 // Sets the shared-memory attribute (outside any capture) and returns CTAs per SM.
-template <typename T, int K, int RX, int RY, int NS>
+template <typename T, int K, int RX, int RY, int NS, bool TMA = false>
 static int occ_f() {
   typedef TileCfg<T, K, RX, RY, NS> G;
-  auto kern = rk4_2d_fused<T, K, RX, RY, NS>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM) != cudaSuccess)
+  auto kern = rk4_2d_fused<T, K, RX, RY, NS, TMA>;
+  const size_t smem = smem_f<T, K, RX, RY, NS, TMA>();
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, G::NT, G::SMEM) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, G::NT, smem) != cudaSuccess) return 0;
   return nb;
+}
+
+template <typename T, int K, int RX, int RY, int NS>
+static cudaError_t launch_ft(const Inst2D* d_insts, const TileItem* d_items, int n_items, int j_step,
+                             int grid, cudaStream_t s) {
+  return launch_f<T, K, RX, RY, NS, true>(d_insts, d_items, n_items, j_step, grid, s);
+}
+template <typename T, int K, int RX, int RY, int NS>
+static int occ_ft() {
+  return occ_f<T, K, RX, RY, NS, true>();
 }
 
 #define NLSG_SHAPES(T, K, CALL, ...)                                        \
@@ -348,17 +511,89 @@ cudaError_t launch_2d_fused(int dtype, int K, int shape, const Inst2D* d_insts,
   return cudaErrorInvalidValue;
 }
 
+// ---- TMA path (complex64): tensor maps, launch, occupancy, wait-timeout flag
+
+int fused_2d_tma_blocks_per_sm(int K, int shape) {
+  if (!tile_supported(shape, NLS_C64)) return 0;
+  if (K == 1) { NLSG_SHAPES(float, 1, occ_ft) }
+  if (K == 2) { NLSG_SHAPES(float, 2, occ_ft) }
+  return 0;
+}
+
+cudaError_t launch_2d_fused_tma(int K, int shape, const Inst2D* d_insts, const TileItem* d_items,
+                                int n_items, int j_step, int grid, cudaStream_t s) {
+  if (n_items <= 0) return cudaSuccess;
+  if (!tile_supported(shape, NLS_C64)) return cudaErrorInvalidValue;
+  if (K == 1) { NLSG_SHAPES(float, 1, launch_ft, d_insts, d_items, n_items, j_step, grid, s) }
+  if (K == 2) { NLSG_SHAPES(float, 2, launch_ft, d_insts, d_items, n_items, j_step, grid, s) }
+  return cudaErrorInvalidValue;
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+bool tma_eligible(int dtype, int n, const void* u0, const void* u1, const void* P) {
+  if (dtype != NLS_C64 || n % 4 != 0) return false;     // row pitch of the pump: multiple of 16 B
+  auto al = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+  return al(u0) && al(u1) && al(P) && encode_fn() != nullptr;
+}
+
+int tma_encode_2d(int shape, int n, const void* u0, const void* u1, const void* P, void* out_maps) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+  if (!enc) return 1;
+  CUtensorMap* m = reinterpret_cast<CUtensorMap*>(out_maps);
+  const cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
+  const cuuint32_t box[2] = {(cuuint32_t)tile_region_x(shape), (cuuint32_t)tile_region_y(shape)};
+  const cuuint32_t estr[2] = {1, 1};
+  const cuuint64_t su[1] = {(cuuint64_t)n * 8};
+  const cuuint64_t sp[1] = {(cuuint64_t)n * 4};
+  const void* srcs[2] = {u0, u1};
+  for (int b = 0; b < 2; ++b)
+    if (enc(&m[b], CU_TENSOR_MAP_DATA_TYPE_INT64, 2, const_cast<void*>(srcs[b]), dims, su, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return 2;
+  if (enc(&m[2], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(P), dims, sp, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return 3;
+  return 0;
+}
+
+size_t tma_map_bytes() { return 3 * sizeof(CUtensorMap); }
+
+int tile_wait_timeout_read_clear(cudaStream_t s) {
+  int v = 0, zero = 0;
+  if (cudaMemcpyFromSymbolAsync(&v, g_tile_wait_timeout, sizeof(int), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return -1;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  if (v) cudaMemcpyToSymbolAsync(g_tile_wait_timeout, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s);
+  return v;
+}
+
 cudaError_t launch_2d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,
                             void* acc, void* dst, double dt, const PhysD& ph, const Stencil2D& op,
                             cudaStream_t st) {
   dim3 grid((n + 31) / 32, (n + 7) / 8);
   if (dtype == NLS_C128) {
-    if (op.K == 1) rk4_2d_stage<double, 1><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, dt, ph, op);
-    else if (op.K == 2) rk4_2d_stage<double, 2><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, dt, ph, op);
+    const Params<double> p = make_params<double>(ph, dt, op.center, op.w[0], op.w[1]);
+    if (op.K == 1) rk4_2d_stage<double, 1><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, p);
+    else if (op.K == 2) rk4_2d_stage<double, 2><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, p);
     else return cudaErrorInvalidValue;
   } else {
-    if (op.K == 1) rk4_2d_stage<float, 1><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, dt, ph, op);
-    else if (op.K == 2) rk4_2d_stage<float, 2><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, dt, ph, op);
+    const Params<float> p = make_params<float>(ph, dt, op.center, op.w[0], op.w[1]);
+    if (op.K == 1) rk4_2d_stage<float, 1><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, p);
+    else if (op.K == 2) rk4_2d_stage<float, 2><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, p);
     else return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -368,12 +603,14 @@ cudaError_t launch_rhs_2d(int dtype, int n, const void* u, const void* P, void* 
                           const Stencil2D& op, cudaStream_t st) {
   dim3 grid((n + 31) / 32, (n + 7) / 8);
   if (dtype == NLS_C128) {
-    if (op.K == 1) rhs_2d<double, 1><<<grid, 256, 0, st>>>(n, u, P, v, ph, op);
-    else if (op.K == 2) rhs_2d<double, 2><<<grid, 256, 0, st>>>(n, u, P, v, ph, op);
+    const Params<double> p = make_params<double>(ph, 0.0, op.center, op.w[0], op.w[1]);
+    if (op.K == 1) rhs_2d<double, 1><<<grid, 256, 0, st>>>(n, u, P, v, p);
+    else if (op.K == 2) rhs_2d<double, 2><<<grid, 256, 0, st>>>(n, u, P, v, p);
     else return cudaErrorInvalidValue;
   } else {
-    if (op.K == 1) rhs_2d<float, 1><<<grid, 256, 0, st>>>(n, u, P, v, ph, op);
-    else if (op.K == 2) rhs_2d<float, 2><<<grid, 256, 0, st>>>(n, u, P, v, ph, op);
+    const Params<float> p = make_params<float>(ph, 0.0, op.center, op.w[0], op.w[1]);
+    if (op.K == 1) rhs_2d<float, 1><<<grid, 256, 0, st>>>(n, u, P, v, p);
+    else if (op.K == 2) rhs_2d<float, 2><<<grid, 256, 0, st>>>(n, u, P, v, p);
     else return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -45,6 +45,16 @@ int fused_2d_blocks_per_sm(int dtype, int K, int shape);
 cudaError_t launch_2d_fused(int dtype, int K, int shape, const Inst2D* d_insts,
                             const TileItem* d_items, int n_items, int j_step, int grid,
                             cudaStream_t s);
+// TMA path of the fused step (complex64 only): one elected thread per CTA prefetches the next
+// tile's state and pump boxes with cp.async.bulk.tensor while the current tile is computed.
+bool tma_eligible(int dtype, int n, const void* u0, const void* u1, const void* P);
+size_t tma_map_bytes();  // bytes of the 3 tensor maps of one instance (128-byte aligned slot)
+int tma_encode_2d(int shape, int n, const void* u0, const void* u1, const void* P, void* out_maps);
+int fused_2d_tma_blocks_per_sm(int K, int shape);
+cudaError_t launch_2d_fused_tma(int K, int shape, const Inst2D* d_insts, const TileItem* d_items,
+                                int n_items, int j_step, int grid, cudaStream_t s);
+// 1 if a bounded tile wait expired since the last call (then cleared), 0 if not, -1 on error
+int tile_wait_timeout_read_clear(cudaStream_t s);
 cudaError_t launch_2d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,
                             void* acc, void* dst, double dt, const PhysD& ph, const Stencil2D& op,
                             cudaStream_t st);

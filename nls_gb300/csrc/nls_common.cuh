@@ -36,6 +36,12 @@ template <typename T> __host__ __device__ inline Phys<T> phys_from(const PhysD& 
   return q;
 }
 
+template <typename T> __device__ __forceinline__ Phys<T> phys_of(const Params<T>& p) {
+  Phys<T> q;
+  q.c3 = p.c3; q.c4 = p.c4; q.c5 = p.c5; q.c6 = p.c6; q.c12 = p.c12; q.c13 = p.c13; q.c14 = p.c14;
+  return q;
+}
+
 // Division in the reservoir term.  Double precision keeps the IEEE quotient of the reference's
 // arithmetic; single precision (the precision form) uses the hardware fast reciprocal-based
 // quotient, which is within 2 ulp and far inside the form's 1e-4 error budget.
@@ -62,11 +68,11 @@ template <typename T> struct RK {
   T half_dt, dt, dt6;
 };
 
-template <typename T> __device__ __forceinline__ RK<T> rk_from(double dt) {
+template <typename T> __device__ __forceinline__ RK<T> rk_of(const Params<T>& p) {
   RK<T> r;
-  r.half_dt = (T)(dt * 0.5);
-  r.dt = (T)dt;
-  r.dt6 = (T)(dt / 6.0);
+  r.half_dt = p.half_dt;
+  r.dt = p.dt;
+  r.dt6 = p.dt6;
   return r;
 }
 

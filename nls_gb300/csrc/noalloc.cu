@@ -26,7 +26,7 @@ using namespace nlsg;
 namespace {
 
 constexpr size_t kStateBytes = (size_t)NLS_NOALLOC_MAX_NODES * 16;  // complex128 worst case
-constexpr size_t kDescBytes = 256;                                   // one Inst2D, padded
+constexpr size_t kDescBytes = 512;                                   // one Inst2D, padded
 constexpr size_t kMaxTiles = 16384;                                  // >= tiles of any allowed grid
 constexpr size_t kTileBytes = kMaxTiles * sizeof(TileItem);
 constexpr size_t kScratchBytes = kStateBytes + kDescBytes + kTileBytes;
@@ -101,6 +101,7 @@ NLS_API int nls_solve_2d_noalloc(int dtype, const nls_problem* pr, int64_t iters
   I.ph.c3 = pr->coeffs[2]; I.ph.c4 = pr->coeffs[3]; I.ph.c5 = pr->coeffs[4]; I.ph.c6 = pr->coeffs[5];
   I.ph.c12 = pr->coeffs[11]; I.ph.c13 = pr->coeffs[12]; I.ph.c14 = pr->coeffs[13];
   I.op = op;
+  set_params(I);
   std::vector<TileItem> items(n_items);
   for (int t = 0; t < n_items; ++t) items[t] = TileItem{0, t};
   // Pageable host sources: each copy returns once its bytes are staged, so the host vectors

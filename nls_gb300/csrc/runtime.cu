@@ -11,6 +11,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/nls_gb300.h"
@@ -55,6 +56,9 @@ struct nls_ctx {
   cudaStream_t stream = nullptr;
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  static constexpr int kSide = 4;    // side streams for concurrent 1-D groups
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t side_done[kSide] = {};
   std::string err;
   std::mutex mu;
   int64_t launches = 0;
@@ -62,6 +66,7 @@ struct nls_ctx {
   DevBuf desc;      // instance descriptors and tile lists of single solves
   DevBuf io;        // uploaded inputs of host-buffer calls
   DevBuf diag;      // diagnostics partials and results
+  DevBuf diagv;     // H(u) scratch of the device chemical potential
   double* h_diag = nullptr;  // pinned
 };
 
@@ -84,6 +89,14 @@ static int fail_cuda(nls_ctx* ctx, cudaError_t e, const char* what) {
   } while (0)
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// A bounded wait inside a tile kernel that expired leaves a device flag; report it once.
+static int check_timeout(nls_ctx* ctx) {
+  const int t = tile_wait_timeout_read_clear(ctx->stream);
+  if (t < 0) return fail(ctx, NLS_ERR_CUDA, "reading the tile-wait flag failed");
+  if (t > 0) return fail(ctx, NLS_ERR_TIMEOUT, "a tile copy did not arrive within its bounded wait");
+  return NLS_OK;
+}
 static size_t csize(int dtype) { return dtype == NLS_C128 ? 16 : 8; }
 static size_t rsize(int dtype) { return dtype == NLS_C128 ? 8 : 4; }
 
@@ -188,6 +201,7 @@ static int solve_1d_dev(nls_ctx* ctx, int dtype, const nls_problem* pr, int64_t 
     Inst1D I;
     std::memset(&I, 0, sizeof(I));
     I.u = u; I.P = P; I.n = n; I.cl = cl; I.steps = iters; I.dt = pr->dt; I.ph = ph; I.op = op;
+    set_params(I);
     CK(ctx, ctx->desc.ensure(sizeof(Inst1D)));
     CK(ctx, cudaMemcpyAsync(ctx->desc.p, &I, sizeof(I), cudaMemcpyHostToDevice, ctx->stream));
     const int seg = (n + cl - 1) / cl;
@@ -257,27 +271,40 @@ static int solve_2d_dev(nls_ctx* ctx, int dtype, const nls_problem* pr, int64_t 
   std::memset(&I, 0, sizeof(I));
   I.u[0] = u; I.u[1] = ctx->scratch.p; I.P = P; I.n = n; I.tiles_x = tiles_x; I.parity = 0;
   I.steps = INT64_MAX; I.dt = pr->dt; I.ph = ph; I.op = op;
+  set_params(I);
   std::vector<TileItem> items(n_items);
   for (int t = 0; t < n_items; ++t) items[t] = TileItem{0, t};
   const size_t ib = align256(sizeof(Inst2D));
-  CK(ctx, ctx->desc.ensure(ib + sizeof(TileItem) * n_items));
+  const size_t tb = align256(sizeof(TileItem) * n_items);
+  const bool tma = tma_eligible(dtype, n, u, ctx->scratch.p, P);
+  CK(ctx, ctx->desc.ensure(ib + tb + (tma ? tma_map_bytes() : 0)));
   Inst2D* dI = (Inst2D*)ctx->desc.p;
   TileItem* dT = (TileItem*)((char*)ctx->desc.p + ib);
+  if (tma) {
+    alignas(128) unsigned char maps[3 * 128];
+    if (tma_encode_2d(shape, n, u, ctx->scratch.p, P, maps)) return fail(ctx, NLS_ERR_CUDA, "tensor map encoding");
+    void* dmaps = (char*)ctx->desc.p + ib + tb;
+    CK(ctx, cudaMemcpyAsync(dmaps, maps, tma_map_bytes(), cudaMemcpyHostToDevice, ctx->stream));
+    I.tmap = dmaps;
+  }
   CK(ctx, cudaMemcpyAsync(dI, &I, sizeof(I), cudaMemcpyHostToDevice, ctx->stream));
   CK(ctx, cudaMemcpyAsync(dT, items.data(), sizeof(TileItem) * n_items, cudaMemcpyHostToDevice, ctx->stream));
-  const int occ = fused_2d_blocks_per_sm(dtype, op.K, shape);
+  const int occ = tma ? fused_2d_tma_blocks_per_sm(op.K, shape) : fused_2d_blocks_per_sm(dtype, op.K, shape);
   const int grid = std::max(1, std::min(n_items, ctx->sm_count * std::max(1, occ)));
+  auto launch = [&](int j) -> cudaError_t {
+    return tma ? launch_2d_fused_tma(op.K, shape, dI, dT, n_items, j, grid, ctx->stream)
+               : launch_2d_fused(dtype, op.K, shape, dI, dT, n_items, j, grid, ctx->stream);
+  };
   const int S = 64;  // even: a replay returns the state to the caller's buffer
   CK(ctx, replay(ctx, iters / S, [&]() -> cudaError_t {
        for (int j = 0; j < S; ++j) {
-         cudaError_t e = launch_2d_fused(dtype, op.K, shape, dI, dT, n_items, j, grid, ctx->stream);
+         cudaError_t e = launch(j);
          if (e) return e;
        }
        return cudaSuccess;
      }));
   const int64_t rem = iters % S;
-  for (int64_t j = 0; j < rem; ++j)
-    CK(ctx, launch_2d_fused(dtype, op.K, shape, dI, dT, n_items, (int)j, grid, ctx->stream));
+  for (int64_t j = 0; j < rem; ++j) CK(ctx, launch((int)j));
   if (rem & 1) CK(ctx, cudaMemcpyAsync(u, ctx->scratch.p, N * csize(dtype), cudaMemcpyDeviceToDevice, ctx->stream));
   ctx->launches += iters;
   return NLS_OK;
@@ -316,7 +343,7 @@ static int solve_host(nls_ctx* ctx, int dtype, int dim, double dt, double dx, in
   if (st) return st;
   CK(ctx, cudaMemcpyAsync(u, du, N * csize(dtype), cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
-  return NLS_OK;
+  return check_timeout(ctx);
 }
 
 // ------------------------------------------------------------------ diagnostics
@@ -329,23 +356,13 @@ static int diag_ensure(nls_ctx* ctx) {
 
 static double* diag_out(nls_ctx* ctx) { return (double*)((char*)ctx->diag.p + diag_partials_bytes(0)); }
 
-static int chem_pot(nls_ctx* ctx, int dtype, int dim, double dx, int n, const double* coeffs,
-                    const void* P, const void* u0, double* s_re, double* s_im, double* m) {
-  if (!ctx) return NLS_ERR_INVALID;
-  std::lock_guard<std::mutex> lk(ctx->mu);
-  if (!coeffs || !P || !u0) return fail(ctx, NLS_ERR_INVALID, "null host pointer");
-  if (dtype != NLS_C128 && dtype != NLS_C64) return fail(ctx, NLS_ERR_INVALID, "bad dtype");
-  if (n < 5) return fail(ctx, NLS_ERR_INVALID, "chemical potential needs n >= 5 (order-5 operator)");
-  CK(ctx, cudaSetDevice(ctx->device));
+// Sums of the chemical potential (nls/nls.f90:921-971) of a device state u: S = sum w conj(u) H(u)
+// and M = sum w |u|^2 (w = r_i in 1-D, 1 in 2-D), FP64, with H evaluated with the order-5
+// operator like the reference.  v is device scratch of the state's size.  Blocks until done.
+static int chem_pot_dev(nls_ctx* ctx, int dtype, int dim, double dx, int n, const double* coeffs,
+                        const void* dP, const void* du, void* dv, double* s_re, double* s_im, double* m) {
   const PhysD ph = phys_of(coeffs);
   const size_t N = dim == 1 ? (size_t)n : (size_t)n * n;
-  const size_t ub = align256(N * csize(dtype)), pb = align256(N * rsize(dtype));
-  CK(ctx, ctx->io.ensure(2 * ub + pb));
-  void* du = ctx->io.p;
-  void* dv = (char*)ctx->io.p + ub;
-  void* dP = (char*)ctx->io.p + 2 * ub;
-  CK(ctx, cudaMemcpyAsync(du, u0, N * csize(dtype), cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(dP, P, N * rsize(dtype), cudaMemcpyHostToDevice, ctx->stream));
   int st = diag_ensure(ctx);
   if (st) return st;
   if (dim == 1) {
@@ -360,11 +377,30 @@ static int chem_pot(nls_ctx* ctx, int dtype, int dim, double dx, int n, const do
   CK(ctx, diag_mu(dtype, (long long)N, du, dv, dim == 1 ? 1 : 0, dx, (double*)ctx->diag.p, diag_out(ctx), ctx->stream));
   CK(ctx, cudaMemcpyAsync(ctx->h_diag, diag_out(ctx), 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
-  ctx->launches += 4;
+  ctx->launches += 3;
   *s_re = ctx->h_diag[0];
   *s_im = ctx->h_diag[1];
   *m = ctx->h_diag[2];
   return NLS_OK;
+}
+
+static int chem_pot(nls_ctx* ctx, int dtype, int dim, double dx, int n, const double* coeffs,
+                    const void* P, const void* u0, double* s_re, double* s_im, double* m) {
+  if (!ctx) return NLS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!coeffs || !P || !u0) return fail(ctx, NLS_ERR_INVALID, "null host pointer");
+  if (dtype != NLS_C128 && dtype != NLS_C64) return fail(ctx, NLS_ERR_INVALID, "bad dtype");
+  if (n < 5) return fail(ctx, NLS_ERR_INVALID, "chemical potential needs n >= 5 (order-5 operator)");
+  CK(ctx, cudaSetDevice(ctx->device));
+  const size_t N = dim == 1 ? (size_t)n : (size_t)n * n;
+  const size_t ub = align256(N * csize(dtype)), pb = align256(N * rsize(dtype));
+  CK(ctx, ctx->io.ensure(2 * ub + pb));
+  void* du = ctx->io.p;
+  void* dv = (char*)ctx->io.p + ub;
+  void* dP = (char*)ctx->io.p + 2 * ub;
+  CK(ctx, cudaMemcpyAsync(du, u0, N * csize(dtype), cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(dP, P, N * rsize(dtype), cudaMemcpyHostToDevice, ctx->stream));
+  return chem_pot_dev(ctx, dtype, dim, dx, n, coeffs, dP, du, dv, s_re, s_im, m);
 }
 
 // ------------------------------------------------------------------ arena allocator
@@ -446,6 +482,8 @@ struct Group2D {
   Inst2D* d = nullptr;
   TileItem* items = nullptr;
   int n_items = 0;
+  bool tma = false;
+  char* maps = nullptr;    // 3 tensor maps per member (TMA path)
 };
 
 struct Member {
@@ -496,7 +534,11 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
       if (cl < 0) return fail(ctx, NLS_ERR_INVALID, "1-D variant not feasible");
       M.kind = cl > 0 ? 1 : 4;
       if (M.kind == 1) {
-        auto k = std::make_pair(M.op1.K, cl);
+        // group by (K, cluster size, segment size class) so a launch sizes its CTAs to its members
+        const int seg = (M.pr.n + cl - 1) / cl;
+        int cls = 64;
+        while (cls < seg) cls *= 2;
+        auto k = std::make_pair(M.op1.K * 1000 + cl, cls);
         if (!key1.count(k)) { key1[k] = (int)b->g1.size(); b->g1.push_back(Group1D{M.op1.K, cl, 0, {}, nullptr}); }
         M.group = key1[k];
         Group1D& G = b->g1[M.group];
@@ -511,7 +553,7 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
       M.kind = shape > 0 ? 2 : 3;
       if (M.kind == 2) {
         auto k = std::make_pair(M.op2.K, shape);
-        if (!key2.count(k)) { key2[k] = (int)b->g2.size(); b->g2.push_back(Group2D{M.op2.K, shape, 0, {}, nullptr, nullptr, 0}); }
+        if (!key2.count(k)) { key2[k] = (int)b->g2.size(); b->g2.push_back(Group2D{M.op2.K, shape, 0, {}, nullptr, nullptr, 0, false, nullptr}); }
         M.group = key2[k];
         b->g2[M.group].idx.push_back(i);
       }
@@ -523,7 +565,7 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
     offs[4 * i + 3] = off; if (M.kind == 3 || M.kind == 4) off += 3 * cb;
   }
   // descriptors
-  std::vector<size_t> g1off(b->g1.size()), g2off(b->g2.size()), g2items(b->g2.size());
+  std::vector<size_t> g1off(b->g1.size()), g2off(b->g2.size()), g2items(b->g2.size()), g2maps;
   for (size_t g = 0; g < b->g1.size(); ++g) { g1off[g] = off; off += align256(sizeof(Inst1D) * b->g1[g].idx.size()); }
   for (size_t g = 0; g < b->g2.size(); ++g) {
     Group2D& G = b->g2[g];
@@ -535,6 +577,7 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
     G.n_items = items;
     g2off[g] = off; off += align256(sizeof(Inst2D) * G.idx.size());
     g2items[g] = off; off += align256(sizeof(TileItem) * std::max(1, items));
+    g2maps.push_back(off); off += align256(tma_map_bytes() * G.idx.size());
   }
   b->mem_bytes = std::max<size_t>(off, 256);
   CK(ctx, cudaMalloc(&b->mem, b->mem_bytes));
@@ -562,7 +605,25 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
     if (!items.empty())
       CK(ctx, cudaMemcpyAsync(G.items, items.data(), sizeof(TileItem) * items.size(), cudaMemcpyHostToDevice,
                               ctx->stream));
-    const int occ = fused_2d_blocks_per_sm(dtype, G.K, G.shape);
+    // TMA path when every member qualifies (complex64, n % 4 == 0, 16-byte aligned buffers)
+    G.maps = b->mem + g2maps[g];
+    G.tma = true;
+    for (int i : G.idx) {
+      const Member& M = b->m[i];
+      G.tma = G.tma && tma_eligible(dtype, M.pr.n, M.u[0], M.u[1], M.P);
+    }
+    if (G.tma) {
+      std::vector<unsigned char> maps(tma_map_bytes() * G.idx.size() + 128);
+      unsigned char* hm = (unsigned char*)(((uintptr_t)maps.data() + 127) & ~(uintptr_t)127);
+      for (size_t k = 0; k < G.idx.size(); ++k) {
+        const Member& M = b->m[G.idx[k]];
+        if (tma_encode_2d(G.shape, M.pr.n, M.u[0], M.u[1], M.P, hm + k * tma_map_bytes()))
+          return fail(ctx, NLS_ERR_CUDA, "tensor map encoding");
+      }
+      CK(ctx, cudaMemcpyAsync(G.maps, hm, tma_map_bytes() * G.idx.size(), cudaMemcpyHostToDevice, ctx->stream));
+      CK(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    const int occ = G.tma ? fused_2d_tma_blocks_per_sm(G.K, G.shape) : fused_2d_blocks_per_sm(dtype, G.K, G.shape);
     G.grid = std::max(1, std::min(G.n_items, ctx->sm_count * std::max(1, occ)));
   }
   for (auto& G : b->g1) CK(ctx, prepare_1d_resident(dtype, G.K, G.cl, G.seg_cap));
@@ -581,6 +642,7 @@ static int batch_descriptors(nls_batch* b, int64_t steps) {
       std::memset(&I, 0, sizeof(I));
       I.u = M.u[0]; I.P = M.P; I.n = M.pr.n; I.cl = G.cl; I.steps = steps; I.dt = M.pr.dt;
       I.ph = phys_of(M.pr.coeffs); I.op = M.op1;
+      set_params(I);
     }
     CK(ctx, cudaMemcpyAsync(G.d, h.data(), sizeof(Inst1D) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
   }
@@ -594,6 +656,8 @@ static int batch_descriptors(nls_batch* b, int64_t steps) {
       I.u[0] = M.u[0]; I.u[1] = M.u[1]; I.P = M.P; I.n = M.pr.n;
       I.tiles_x = (M.pr.n + tx - 1) / tx; I.parity = M.parity; I.steps = INT64_MAX; I.dt = M.pr.dt;
       I.ph = phys_of(M.pr.coeffs); I.op = M.op2;
+      I.tmap = G.tma ? G.maps + k * tma_map_bytes() : nullptr;
+      set_params(I);
     }
     CK(ctx, cudaMemcpyAsync(G.d, h.data(), sizeof(Inst2D) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
   }
@@ -605,15 +669,23 @@ static cudaError_t batch_sequence(nls_batch* b, int64_t steps) {
   const int dtype = b->dtype;
   cudaError_t e;
   const bool fork = !b->g1.empty();
+  const int nside = std::min<int>(nls_ctx::kSide, (int)b->g1.size());
   if (fork) {
+    // the 1-D groups run concurrently on side streams while the main stream steps the 2-D tiles
     if ((e = cudaEventRecord(ctx->ev_fork, ctx->stream))) return e;
-    if ((e = cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0))) return e;
-    for (auto& G : b->g1)
-      if ((e = launch_1d_resident(dtype, G.K, G.d, (int)G.idx.size(), G.cl, G.seg_cap, ctx->aux))) return e;
+    for (int i = 0; i < nside; ++i)
+      if ((e = cudaStreamWaitEvent(ctx->side[i], ctx->ev_fork, 0))) return e;
+    for (size_t g = 0; g < b->g1.size(); ++g) {
+      auto& G = b->g1[g];
+      if ((e = launch_1d_resident(dtype, G.K, G.d, (int)G.idx.size(), G.cl, G.seg_cap, ctx->side[g % nside])))
+        return e;
+    }
   }
   for (int64_t j = 0; j < steps; ++j) {
     for (auto& G : b->g2)
-      if ((e = launch_2d_fused(dtype, G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream))) return e;
+      if ((e = G.tma ? launch_2d_fused_tma(G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream)
+                     : launch_2d_fused(dtype, G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream)))
+        return e;
     for (auto& M : b->m) {
       if (M.kind != 3) continue;
       const size_t cb = align256(M.N * csize(dtype));
@@ -640,8 +712,10 @@ static cudaError_t batch_sequence(nls_batch* b, int64_t steps) {
     }
   }
   if (fork) {
-    if ((e = cudaEventRecord(ctx->ev_join, ctx->aux))) return e;
-    if ((e = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0))) return e;
+    for (int i = 0; i < nside; ++i) {
+      if ((e = cudaEventRecord(ctx->side_done[i], ctx->side[i]))) return e;
+      if ((e = cudaStreamWaitEvent(ctx->stream, ctx->side_done[i], 0))) return e;
+    }
   }
   return cudaSuccess;
 }
@@ -668,6 +742,8 @@ struct Slot {
   Stencil1D op1;
   Stencil2D op2;
   uint64_t finish_seq = 0;
+  bool tma = false;
+  std::vector<unsigned char> maps;   // 3 tensor maps (host copy), when tma
 };
 
 struct nls_pool {
@@ -724,6 +800,13 @@ NLS_API int nls_ctx_create(int device, nls_ctx** out) {
     delete ctx;
     return NLS_ERR_CUDA;
   }
+  for (int i = 0; i < nls_ctx::kSide; ++i) {
+    if (cudaStreamCreateWithFlags(&ctx->side[i], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->side_done[i], cudaEventDisableTiming) != cudaSuccess) {
+      delete ctx;
+      return NLS_ERR_CUDA;
+    }
+  }
   *out = ctx;
   return NLS_OK;
 }
@@ -737,9 +820,15 @@ NLS_API int nls_ctx_destroy(nls_ctx* ctx) {
   ctx->desc.release();
   ctx->io.release();
   ctx->diag.release();
+  ctx->diagv.release();
   if (ctx->h_diag) cudaFreeHost(ctx->h_diag);
   cudaEventDestroy(ctx->ev_fork);
   cudaEventDestroy(ctx->ev_join);
+  for (int i = 0; i < nls_ctx::kSide; ++i) {
+    cudaStreamSynchronize(ctx->side[i]);
+    cudaEventDestroy(ctx->side_done[i]);
+    cudaStreamDestroy(ctx->side[i]);
+  }
   cudaStreamDestroy(ctx->aux);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -756,7 +845,7 @@ NLS_API int nls_ctx_synchronize(nls_ctx* ctx) {
   if (!ctx) return NLS_ERR_INVALID;
   CK(ctx, cudaSetDevice(ctx->device));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
-  return NLS_OK;
+  return check_timeout(ctx);
 }
 
 NLS_API const char* nls_last_error(nls_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
@@ -799,6 +888,24 @@ NLS_API int nls_chemical_potential_2d(nls_ctx* ctx, int dtype, double dx, int n,
   int st = chem_pot(ctx, dtype, 2, dx, n, coeffs23, pumping, u0, &sr, &si, &m);
   if (st) return st;
   *mu = -si / m;  // real part of i S / M (nls/nls.f90:967-970)
+  return NLS_OK;
+}
+
+NLS_API int nls_chemical_potential_device(nls_ctx* ctx, int dtype, const nls_problem* pr, const void* pumping_dev,
+                                          const void* u_dev, double* mu_re, double* mu_im) {
+  if (!ctx) return NLS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!pr || !pumping_dev || !u_dev || !mu_re || !mu_im) return fail(ctx, NLS_ERR_INVALID, "bad arguments");
+  if (dtype != NLS_C128 && dtype != NLS_C64) return fail(ctx, NLS_ERR_INVALID, "bad dtype");
+  if ((pr->dim != 1 && pr->dim != 2) || pr->n < 5) return fail(ctx, NLS_ERR_INVALID, "dim 1 or 2 and n >= 5");
+  CK(ctx, cudaSetDevice(ctx->device));
+  const size_t N = pr->dim == 1 ? (size_t)pr->n : (size_t)pr->n * pr->n;
+  CK(ctx, ctx->diagv.ensure(N * csize(dtype)));
+  double sr, si, m;
+  int st = chem_pot_dev(ctx, dtype, pr->dim, pr->dx, pr->n, pr->coeffs, pumping_dev, u_dev, ctx->diagv.p, &sr, &si, &m);
+  if (st) return st;
+  *mu_re = -si / m;   // mu = i S / M
+  *mu_im = sr / m;
   return NLS_OK;
 }
 
@@ -1023,6 +1130,14 @@ NLS_API int nls_pool_admit(nls_pool* p, const nls_problem* problem, const void* 
   S.remaining = steps;
   S.parity = 0;
   if (S.done) S.finish_seq = ++p->seq;
+  if (S.kind == 2 && tma_eligible(p->dtype, S.pr.n, S.u[0], S.u[1], S.P)) {
+    std::vector<unsigned char> buf(tma_map_bytes() + 128);
+    unsigned char* hm = (unsigned char*)(((uintptr_t)buf.data() + 127) & ~(uintptr_t)127);
+    if (tma_encode_2d(S.shape, S.pr.n, S.u[0], S.u[1], S.P, hm) == 0) {
+      S.tma = true;
+      S.maps.assign(hm, hm + tma_map_bytes());
+    }
+  }
   cudaError_t e1 = cudaMemcpyAsync(S.P, pumping, S.N * rsize(p->dtype), cudaMemcpyHostToDevice, ctx->stream);
   cudaError_t e2 = cudaMemcpyAsync(S.u[0], u0, S.N * csize(p->dtype), cudaMemcpyHostToDevice, ctx->stream);
   cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
@@ -1042,13 +1157,14 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
   CK(ctx, cudaSetDevice(ctx->device));
   const int dtype = p->dtype;
   // group the active slots
-  std::map<std::pair<int, int>, std::vector<int>> g1, g2;
+  std::map<std::pair<int, int>, std::vector<int>> g1;
+  std::map<std::tuple<int, int, int>, std::vector<int>> g2;   // (K, shape, tma)
   int64_t max_steps = 0;
   for (size_t i = 0; i < p->slots.size(); ++i) {
     const Slot& S = p->slots[i];
     if (!S.used || S.done) continue;
     if (S.kind == 1) g1[{S.K, S.cl}].push_back((int)i);
-    else g2[{S.K, S.shape}].push_back((int)i);
+    else g2[std::make_tuple(S.K, S.shape, S.tma ? 1 : 0)].push_back((int)i);
     max_steps = std::max<int64_t>(max_steps, std::min<int64_t>(S.remaining, p->chunk));
   }
   if (finished) *finished = 0;
@@ -1059,12 +1175,13 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
   for (auto& kv : g2) {
     int items = 0;
     for (int i : kv.second) items += p->slots[i].ntiles;
-    bytes += align256(sizeof(Inst2D) * kv.second.size()) + align256(sizeof(TileItem) * items);
+    bytes += align256(sizeof(Inst2D) * kv.second.size()) + align256(sizeof(TileItem) * items) +
+             align256(tma_map_bytes() * kv.second.size());
   }
   p->h_desc.assign(bytes, 0);
   CK(ctx, p->d_desc.ensure(bytes));
   struct L1 { int K, cl, seg, count; size_t off; };
-  struct L2 { int K, shape, n_items, grid; size_t off, off_items; };
+  struct L2 { int K, shape, n_items, grid; size_t off, off_items; bool tma; };
   std::vector<L1> l1;
   std::vector<L2> l2;
   size_t off = 0;
@@ -1077,28 +1194,39 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
       I.u = S.u[0]; I.P = S.P; I.n = S.pr.n; I.cl = S.cl;
       I.steps = std::min<int64_t>(S.remaining, p->chunk);
       I.dt = S.pr.dt; I.ph = phys_of(S.pr.coeffs); I.op = S.op1;
+      set_params(I);
       seg = std::max(seg, (S.pr.n + S.cl - 1) / S.cl);
     }
     l1.push_back(L1{kv.first.first, kv.first.second, seg, (int)kv.second.size(), off});
     off += align256(sizeof(Inst1D) * kv.second.size());
   }
   for (auto& kv : g2) {
+    const int K = std::get<0>(kv.first), shape = std::get<1>(kv.first);
+    const bool tma = std::get<2>(kv.first) != 0;
     Inst2D* h = (Inst2D*)(p->h_desc.data() + off);
     const size_t ioff = off + align256(sizeof(Inst2D) * kv.second.size());
     TileItem* it = (TileItem*)(p->h_desc.data() + ioff);
     int items = 0;
+    for (int i : kv.second) items += p->slots[i].ntiles;
+    const size_t moff = ioff + align256(sizeof(TileItem) * items);
+    items = 0;
     for (size_t k = 0; k < kv.second.size(); ++k) {
       const Slot& S = p->slots[kv.second[k]];
       Inst2D& I = h[k];
       I.u[0] = S.u[0]; I.u[1] = S.u[1]; I.P = S.P; I.n = S.pr.n; I.tiles_x = S.tiles_x;
       I.parity = S.parity; I.steps = std::min<int64_t>(S.remaining, p->chunk);
       I.dt = S.pr.dt; I.ph = phys_of(S.pr.coeffs); I.op = S.op2;
+      set_params(I);
+      if (tma) {
+        std::memcpy(p->h_desc.data() + moff + k * tma_map_bytes(), S.maps.data(), tma_map_bytes());
+        I.tmap = (char*)p->d_desc.p + moff + k * tma_map_bytes();
+      }
       for (int q = 0; q < S.ntiles; ++q) it[items++] = TileItem{(int)k, q};
     }
-    const int occ = fused_2d_blocks_per_sm(dtype, kv.first.first, kv.first.second);
+    const int occ = tma ? fused_2d_tma_blocks_per_sm(K, shape) : fused_2d_blocks_per_sm(dtype, K, shape);
     const int grid = std::max(1, std::min(items, ctx->sm_count * std::max(1, occ)));
-    l2.push_back(L2{kv.first.first, kv.first.second, items, grid, off, ioff});
-    off = ioff + align256(sizeof(TileItem) * items);
+    l2.push_back(L2{K, shape, items, grid, off, ioff, tma});
+    off = moff + align256(tma_map_bytes() * kv.second.size());
   }
   char* d = (char*)p->d_desc.p;
   CK(ctx, cudaMemcpyAsync(d, p->h_desc.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
@@ -1112,8 +1240,10 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
   }
   for (int64_t j = 0; j < max_steps; ++j)
     for (auto& L : l2) {
-      CK(ctx, launch_2d_fused(dtype, L.K, L.shape, (const Inst2D*)(d + L.off), (const TileItem*)(d + L.off_items),
-                              L.n_items, (int)j, L.grid, ctx->stream));
+      const Inst2D* dI = (const Inst2D*)(d + L.off);
+      const TileItem* dT = (const TileItem*)(d + L.off_items);
+      CK(ctx, L.tma ? launch_2d_fused_tma(L.K, L.shape, dI, dT, L.n_items, (int)j, L.grid, ctx->stream)
+                    : launch_2d_fused(dtype, L.K, L.shape, dI, dT, L.n_items, (int)j, L.grid, ctx->stream));
       ctx->launches += 1;
     }
   if (!l1.empty()) {
@@ -1121,6 +1251,10 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
     CK(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
   }
   CK(ctx, cudaStreamSynchronize(ctx->stream));
+  {
+    int st = check_timeout(ctx);
+    if (st) return st;
+  }
   int done = 0;
   for (auto& S : p->slots) {
     if (!S.used || S.done) continue;

@@ -86,6 +86,21 @@ def norm(u: torch.Tensor) -> float:
     return s.value
 
 
+def chemical_potential(u: torch.Tensor, P: torch.Tensor, *, dx: float, coeffs) -> complex:
+    """FP64 chemical potential mu = i<u, H u>/<u, u> of a device state (order-5 operator, radial
+    weight in 1-D), as chemical_potential_1d/2d of the reference (nls/nls.f90:921-971)."""
+    ctx = context(u.device.index or 0)
+    ext = _ext_stream(ctx)
+    ext.wait_stream(torch.cuda.current_stream(u.device))
+    pr = _lib.make_problem(u.dim(), u.shape[0], 5, 0.0, dx, coeffs)
+    re, im = ctypes.c_double(), ctypes.c_double()
+    st = _lib.lib().nls_chemical_potential_device(ctx.handle, _code_of(u), ctypes.byref(pr),
+                                                  ctypes.c_void_p(P.data_ptr()), ctypes.c_void_p(u.data_ptr()),
+                                                  ctypes.byref(re), ctypes.byref(im))
+    _lib.check(st, "nls_chemical_potential_device", ctx.handle)
+    return complex(re.value, im.value)
+
+
 def density_errors(u: torch.Tensor, u_ref: torch.Tensor, P64: torch.Tensor, coeffs):
     """Relative L2 errors of |u|^2 and of the reservoir n against a complex128 reference."""
     if u_ref.dtype != torch.complex128 or P64.dtype != torch.float64:

@@ -304,3 +304,19 @@ def test_pool_same_alone_and_in_the_mix(gpu):
     # and equal to a plain single solve on the same kernel
     want = _device_solve(gpu, target, 123, np.complex64, -1)
     assert np.array_equal(rm[0], want)
+
+
+def test_precision_form_with_fp64_diagnostics(gpu, oracle_lib):
+    """complex64 solve with FP64 norm/chemical-potential logging, checked against complex128."""
+    from nls_gb300 import precision, workloads
+    s, _ = workloads.precision_2d(n=192, length=192 * 0.078125)
+    res = precision.run(s, steps=1200, log_every=500)
+    assert [e["step"] for e in res["log"]] == [500, 1000, 1200]
+    assert all(np.isfinite(e["norm"]) and np.isfinite(e["mu"]) for e in res["log"])
+    assert abs(res["log"][-1]["t"] - 1200 * s.dt) < 1e-15
+    assert res["rel_l2_density"] <= 1e-4 and res["rel_l2_reservoir"] <= 1e-4
+    # the FP64 diagnostics agree with the oracle's chemical potential of the final state
+    u = res["state"].cpu().numpy().T.astype(np.complex128)
+    want = oracle_lib.chemical_potential(s.dx, s.pumping, s.coeffs, u, dtype=np.float64)
+    assert abs(res["log"][-1]["mu"] - want) <= 1e-5 * abs(want)
+    np.testing.assert_allclose(res["log"][-1]["norm"], np.sum(np.abs(u) ** 2) * s.dx ** 2, rtol=1e-12)
