@@ -286,6 +286,10 @@ def run_ours(args):
     from nls_gb300.native import nls
 
     specs = workloads.batch_mix()
+    if args.batch_variant is not None:
+        for sp in specs:
+            if sp.dim == 2:
+                sp.variant = args.batch_variant
     total_nodes = sum(s.nodes for s in specs)
     nodes_2d = sum(s.nodes for s in specs if s.dim == 2)
     b = BatchSolver(specs, dtype=np.complex64, device=local)
@@ -353,7 +357,7 @@ def run_ours(args):
     tpn = _traffic_per_node()
     result["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": (tpn * nodes_2d if tpn else None),
-                          "kernel": "rk4_2d_fused<float,K=1,64x64> over all 2-D tiles, one launch per RK4 step",
+                          "kernel": "rk4_2d_fused<float,K=1,64x72,TMA> over all 2-D tiles, one launch per RK4 step",
                           "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": launch_s * 1e6,
                           "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"}
     b2.close()
@@ -456,6 +460,7 @@ def main():
     ap.add_argument("--order", type=int, default=3, help="stencil order for grid1d/grid2d")
     ap.add_argument("--variant", type=int, default=-1, help="kernel variant for grid1d/grid2d")
     ap.add_argument("--c128", action="store_true", help="complex128 state for grid1d/grid2d")
+    ap.add_argument("--batch-variant", type=int, default=None, help="2-D kernel variant for the batch")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

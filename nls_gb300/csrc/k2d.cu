@@ -75,7 +75,8 @@ struct TileCfg {
   // CTAs per SM the register budget is sized for: 2 x 256 threads, else one CTA
   static constexpr int MINB = NT <= 256 ? 2 : 1;
   // rows per shared-memory load batch in a stage, sized to the register budget
-  static constexpr int CJ = (NT >= 1024 || sizeof(T) == 8) ? 2 : (NJ < 4 ? NJ : 4);
+  static constexpr int CJMAX = (NT >= 1024 || sizeof(T) == 8) ? 2 : 4;
+  static constexpr int CJ = (CJMAX >= 4 && NJ % 4 == 0) ? 4 : (CJMAX >= 3 && NJ % 3 == 0) ? 3 : (NJ % 2 == 0 ? 2 : 1);
   static_assert(RX % 32 == 0 && RY % NS == 0 && NJ <= 32, "tile layout");
   static_assert(TX > 0 && TY > 0, "tile too small for its halo");
 };
@@ -412,25 +413,29 @@ __global__ void __launch_bounds__(256) rhs_2d(int n, const void* __restrict__ u_
 //   TILE_32x32   : 32 x 32,  8 strips of 4 rows  (256 threads)
 //   TILE_64x64W  : 64 x 64,  16 strips of 4 rows (1024 threads)
 //   TILE_128x32W : 128 x 32, 8 strips of 4 rows  (1024 threads)
+//   TILE_64xO64  : 64 x (64 + 8K), 8 strips (512 threads): output tiles exactly 64 rows high
 int tile_region_x(int shape) {
   switch (shape) {
     case TILE_64x64: return 64; case TILE_128x32: return 128; case TILE_32x32: return 32;
     case TILE_64x64W: return 64; case TILE_128x32W: return 128;
+    case TILE_64xO64: return 64;
   }
   return 0;
 }
-int tile_region_y(int shape) {
+int tile_region_y(int shape, int K) {
   switch (shape) {
     case TILE_64x64: return 64; case TILE_128x32: return 32; case TILE_32x32: return 32;
     case TILE_64x64W: return 64; case TILE_128x32W: return 32;
+    case TILE_64xO64: return 64 + 8 * K;
   }
   return 0;
 }
 int tile_out_x(int shape, int K) { return tile_region_x(shape) - 8 * K; }
-int tile_out_y(int shape, int K) { return tile_region_y(shape) - 8 * K; }
+int tile_out_y(int shape, int K) { return tile_region_y(shape, K) - 8 * K; }
 bool tile_supported(int shape, int dtype) {
   if (shape == TILE_32x32) return true;
-  if (shape == TILE_64x64 || shape == TILE_128x32 || shape == TILE_64x64W || shape == TILE_128x32W)
+  if (shape == TILE_64x64 || shape == TILE_128x32 || shape == TILE_64x64W || shape == TILE_128x32W ||
+      shape == TILE_64xO64)
     return dtype == NLS_C64;
   return false;
 }
@@ -480,6 +485,7 @@ static int occ_ft() {
     case TILE_32x32: return CALL<T, K, 32, 32, 8>(__VA_ARGS__);            \
     case TILE_64x64W: return CALL<T, K, 64, 64, 16>(__VA_ARGS__);          \
     case TILE_128x32W: return CALL<T, K, 128, 32, 8>(__VA_ARGS__);         \
+    case TILE_64xO64: return CALL<T, K, 64, 64 + 8 * K, 8>(__VA_ARGS__);   \
   }
 
 int fused_2d_blocks_per_sm(int dtype, int K, int shape) {
@@ -548,12 +554,12 @@ bool tma_eligible(int dtype, int n, const void* u0, const void* u1, const void* 
   return al(u0) && al(u1) && al(P) && encode_fn() != nullptr;
 }
 
-int tma_encode_2d(int shape, int n, const void* u0, const void* u1, const void* P, void* out_maps) {
+int tma_encode_2d(int shape, int K, int n, const void* u0, const void* u1, const void* P, void* out_maps) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc) return 1;
   CUtensorMap* m = reinterpret_cast<CUtensorMap*>(out_maps);
   const cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
-  const cuuint32_t box[2] = {(cuuint32_t)tile_region_x(shape), (cuuint32_t)tile_region_y(shape)};
+  const cuuint32_t box[2] = {(cuuint32_t)tile_region_x(shape), (cuuint32_t)tile_region_y(shape, K)};
   const cuuint32_t estr[2] = {1, 1};
   const cuuint64_t su[1] = {(cuuint64_t)n * 8};
   const cuuint64_t sp[1] = {(cuuint64_t)n * 4};

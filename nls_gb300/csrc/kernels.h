@@ -34,9 +34,10 @@ enum TileShape2D {
   TILE_32x32 = 3,     // region 32 x 32, 256 threads (either precision)
   TILE_64x64W = 4,    // region 64 x 64, 1024 threads (single precision)
   TILE_128x32W = 5,   // region 128 x 32, 1024 threads (single precision)
+  TILE_64xO64 = 6,    // region 64 x (64 + 8K): output tiles 64 rows high, 512 threads
 };
 int tile_region_x(int shape);
-int tile_region_y(int shape);
+int tile_region_y(int shape, int K);
 int tile_out_x(int shape, int K);
 int tile_out_y(int shape, int K);
 bool tile_supported(int shape, int dtype);
@@ -49,7 +50,7 @@ cudaError_t launch_2d_fused(int dtype, int K, int shape, const Inst2D* d_insts,
 // tile's state and pump boxes with cp.async.bulk.tensor while the current tile is computed.
 bool tma_eligible(int dtype, int n, const void* u0, const void* u1, const void* P);
 size_t tma_map_bytes();  // bytes of the 3 tensor maps of one instance (128-byte aligned slot)
-int tma_encode_2d(int shape, int n, const void* u0, const void* u1, const void* P, void* out_maps);
+int tma_encode_2d(int shape, int K, int n, const void* u0, const void* u1, const void* P, void* out_maps);
 int fused_2d_tma_blocks_per_sm(int K, int shape);
 cudaError_t launch_2d_fused_tma(int K, int shape, const Inst2D* d_insts, const TileItem* d_items,
                                 int n_items, int j_step, int grid, cudaStream_t s);

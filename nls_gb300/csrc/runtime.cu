@@ -157,7 +157,7 @@ static int choose_shape(int dtype, int n, int K, int variant) {
     if (!tile_supported(variant, dtype)) return -1;
     return variant;
   }
-  if (dtype == NLS_C64) return TILE_64x64;
+  if (dtype == NLS_C64) return TILE_64xO64;
   return (K == 1 && n >= 1024) ? TILE_32x32 : TILE_UNFUSED;
 }
 
@@ -282,7 +282,7 @@ static int solve_2d_dev(nls_ctx* ctx, int dtype, const nls_problem* pr, int64_t 
   TileItem* dT = (TileItem*)((char*)ctx->desc.p + ib);
   if (tma) {
     alignas(128) unsigned char maps[3 * 128];
-    if (tma_encode_2d(shape, n, u, ctx->scratch.p, P, maps)) return fail(ctx, NLS_ERR_CUDA, "tensor map encoding");
+    if (tma_encode_2d(shape, op.K, n, u, ctx->scratch.p, P, maps)) return fail(ctx, NLS_ERR_CUDA, "tensor map encoding");
     void* dmaps = (char*)ctx->desc.p + ib + tb;
     CK(ctx, cudaMemcpyAsync(dmaps, maps, tma_map_bytes(), cudaMemcpyHostToDevice, ctx->stream));
     I.tmap = dmaps;
@@ -617,7 +617,7 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
       unsigned char* hm = (unsigned char*)(((uintptr_t)maps.data() + 127) & ~(uintptr_t)127);
       for (size_t k = 0; k < G.idx.size(); ++k) {
         const Member& M = b->m[G.idx[k]];
-        if (tma_encode_2d(G.shape, M.pr.n, M.u[0], M.u[1], M.P, hm + k * tma_map_bytes()))
+        if (tma_encode_2d(G.shape, G.K, M.pr.n, M.u[0], M.u[1], M.P, hm + k * tma_map_bytes()))
           return fail(ctx, NLS_ERR_CUDA, "tensor map encoding");
       }
       CK(ctx, cudaMemcpyAsync(G.maps, hm, tma_map_bytes() * G.idx.size(), cudaMemcpyHostToDevice, ctx->stream));
@@ -1133,7 +1133,7 @@ NLS_API int nls_pool_admit(nls_pool* p, const nls_problem* problem, const void* 
   if (S.kind == 2 && tma_eligible(p->dtype, S.pr.n, S.u[0], S.u[1], S.P)) {
     std::vector<unsigned char> buf(tma_map_bytes() + 128);
     unsigned char* hm = (unsigned char*)(((uintptr_t)buf.data() + 127) & ~(uintptr_t)127);
-    if (tma_encode_2d(S.shape, S.pr.n, S.u[0], S.u[1], S.P, hm) == 0) {
+    if (tma_encode_2d(S.shape, S.K, S.pr.n, S.u[0], S.u[1], S.P, hm) == 0) {
       S.tma = true;
       S.maps.assign(hm, hm + tma_map_bytes());
     }
