@@ -166,7 +166,7 @@ def oracle_sample(specs):
     return [s for i, s in enumerate(specs) if i % 4 == 0]
 
 
-def calibrated_steps(specs, threads, target_s=12.0):
+def calibrated_steps(specs, threads, target_s=20.0):
     """RK4 steps per CPU sample so that one sample takes about target_s seconds."""
     _, t1 = cpu_oracle_rate(specs, 1, threads)
     return int(min(2000, max(1, round(target_s / max(t1, 1e-3)))))
@@ -273,6 +273,47 @@ def run_precision(args):
     return 0
 
 
+def run_serve(args):
+    """--workload serve: a Poisson stream of requests (default 10 000 at 200 req/s) drawn from the
+    mixed 1-D/2-D distribution with 1000-20000 steps each, complex64 state, 80 GB admission budget,
+    continuously batched; p50/p99 latency and node-steps/s, next to sequential plain complex128
+    solves of a sample of the same requests."""
+    import torch
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    from nls_gb300 import build as nbuild
+    nbuild.build()
+    from nls_gb300 import device as ndev
+    from nls_gb300 import workloads
+    from nls_gb300.serve import Pool, serve
+    count = args.serve if args.serve > 0 else 10000
+    reqs = workloads.serve_stream(count)
+    pool = Pool(dtype=np.complex64, budget_bytes=80 << 30, chunk_steps=args.chunk, device=local)
+    st = serve(reqs, rate=200.0, pool=pool)
+    pool.close()
+    # sequential plain complex128 solves of a sample of the same requests
+    dev = torch.device("cuda", local)
+    plain_ns, plain_s = 0.0, 0.0
+    for spec, steps in reqs[:: max(1, count // 24)][:24]:
+        u = torch.tensor(np.ascontiguousarray(spec.u0), dtype=torch.complex128, device=dev)
+        P = torch.tensor(np.ascontiguousarray(spec.pumping), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        ndev.solve_(u, P, order=spec.order, dt=spec.dt, dx=spec.dx, coeffs=spec.coeffs, iters=steps)
+        torch.cuda.synchronize(dev)
+        plain_s += time.perf_counter() - t0
+        plain_ns += float(spec.nodes) * steps
+    lat = st["latency_s"]
+    print(json.dumps({"workload": f"serve: {count} requests, Poisson 200/s, steps U[1000,20000], complex64, "
+                                  f"80 GB budget, chunk {args.chunk} steps",
+                      "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": float(np.mean(lat) * 1e3),
+                      "max_ms": float(np.max(lat) * 1e3), "wall_s": st["wall_s"],
+                      "node_steps_per_s": st["node_steps_per_s"], "node_steps": st["node_steps"],
+                      "plain_c128_sequential_node_steps_per_s": plain_ns / plain_s,
+                      "plain_c128_sample": "24 requests of the stream solved one after another"}))
+    return 0
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_init()
@@ -286,10 +327,14 @@ def run_ours(args):
     from nls_gb300.native import nls
 
     specs = workloads.batch_mix()
+    tuned = None
     if args.batch_variant is not None:
         for sp in specs:
             if sp.dim == 2:
                 sp.variant = args.batch_variant
+    elif args.autotune:
+        from nls_gb300 import autotune
+        tuned = autotune.apply(specs, dtype=np.complex64, device=local, mode="batch")
     total_nodes = sum(s.nodes for s in specs)
     nodes_2d = sum(s.nodes for s in specs if s.dim == 2)
     b = BatchSolver(specs, dtype=np.complex64, device=local)
@@ -333,6 +378,8 @@ def run_ours(args):
         "gpu_launches": int(gpu_launches),
         "clocks": clocks,
     }
+    if tuned:
+        result["config"]["autotuned_variants"] = tuned
     if rank != 0:
         return 0
     if args.quick:
@@ -454,18 +501,23 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
     ap.add_argument("--quick", action="store_true",
                     help="timed batched solves only (no roofline, accuracy, e2e, serve or CPU legs)")
-    ap.add_argument("--workload", choices=["batch", "grid1d", "grid2d", "precision2d"], default="batch")
+    ap.add_argument("--workload", choices=["batch", "grid1d", "grid2d", "precision2d", "serve"], default="batch")
+    ap.add_argument("--chunk", type=int, default=500, help="serving pool chunk (RK4 steps per scheduling round)")
     ap.add_argument("--solve-steps", type=int, default=SOLVE_STEPS, help="RK4 steps per solve")
     ap.add_argument("--n", type=int, default=4096, help="grid size for grid1d/grid2d")
     ap.add_argument("--order", type=int, default=3, help="stencil order for grid1d/grid2d")
     ap.add_argument("--variant", type=int, default=-1, help="kernel variant for grid1d/grid2d")
     ap.add_argument("--c128", action="store_true", help="complex128 state for grid1d/grid2d")
     ap.add_argument("--batch-variant", type=int, default=None, help="2-D kernel variant for the batch")
+    ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
+                    help="choose kernel variants per size with the batch-throughput autotuner")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "precision2d":
         return run_precision(args)
+    if args.workload == "serve":
+        return run_serve(args)
     if args.workload != "batch":
         return run_grid(args)
     return run_ours(args)

@@ -8,9 +8,12 @@ variants on a seeded instance of that size and keeps the fastest:
   64x64 / 1024 (4) or 128x32 / 1024 (5);
 * 1-D: the resident kernel on 1, 2, 4, 8 or 16 CTAs of a cluster, or 0 = unfused stage kernels.
 
-Results are cached per GPU name in a JSON file (``NLS_GB300_TUNE_CACHE`` or
-``~/.cache/nls_gb300/autotune.json``); ``apply(specs, dtype)`` fills ``Spec.variant`` for a
-batch.  Timings use CUDA events on the library's stream.
+Two objectives: ``mode="single"`` times one solve of the size (latency of a lone solve), and
+``mode="batch"`` times a batch of copies large enough to fill the GPU (throughput per node-step,
+what a batched or served mix cares about: a shape with less halo recomputation wins there even
+when it exposes fewer tiles per grid).  Results are cached per GPU name in a JSON file
+(``NLS_GB300_TUNE_CACHE`` or ``~/.cache/nls_gb300/autotune.json``); ``apply(specs, dtype, mode)``
+fills ``Spec.variant``.  Timings use CUDA events on the library's stream.
 """
 
 from __future__ import annotations
@@ -74,11 +77,39 @@ def _time_variant(dim, n, order, dtype, variant, steps, device):
     return e0.elapsed_time(e1) / steps
 
 
-def tune(dim: int, n: int, order: int, dtype=np.complex64, steps: int = 128, device: int = 0):
+def _time_batch(dim, n, order, dtype, variant, steps, device):
+    """ms per node-step of a batch of copies of this size with the given variant."""
+    import torch
+
+    from . import device as ndev
+    from . import workloads
+    from .batch import BatchSolver
+    if dim == 2:
+        s, _ = workloads.plain_2d(n=n, length=n * 0.15625, order=order)
+    else:
+        s, _ = workloads.plain_1d(n=n, length=n * 0.04, order=order)
+    s.variant = variant
+    copies = max(1, min(512, (8 << 20) // max(1, s.nodes)))
+    b = BatchSolver([s] * copies, dtype=dtype, device=device)
+    try:
+        b.run(steps)
+        ext = ndev.stream(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        b.run(steps)
+        e1.record(ext)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / (steps * copies * s.nodes)
+    finally:
+        b.close()
+
+
+def tune(dim: int, n: int, order: int, dtype=np.complex64, steps: int = 128, device: int = 0,
+         mode: str = "single"):
     """Fastest variant for this case (cached)."""
     import torch
     name = torch.cuda.get_device_name(device)
-    key = f"{name}|{dim}|{np.dtype(dtype).name}|{order}|{bucket(n)}"
+    key = f"{name}|{mode}|{dim}|{np.dtype(dtype).name}|{order}|{bucket(n)}"
     path = _cache_path()
     with _lock:
         cache = {}
@@ -92,9 +123,12 @@ def tune(dim: int, n: int, order: int, dtype=np.complex64, steps: int = 128, dev
             return int(cache[key]["variant"])
     times = {}
     nb = bucket(n)
+    timer = _time_batch if mode == "batch" else _time_variant
     for v in candidates(dim, dtype, nb):
+        if mode == "batch" and v == 0:
+            continue          # the unfused path is a single-solve fallback
         try:
-            times[v] = _time_variant(dim, nb, order, dtype, v, steps, device)
+            times[v] = timer(dim, nb, order, dtype, v, steps, device)
         except ValueError:
             continue
     best = min(times, key=times.get)
@@ -108,12 +142,12 @@ def tune(dim: int, n: int, order: int, dtype=np.complex64, steps: int = 128, dev
     return int(best)
 
 
-def apply(specs, dtype=np.complex64, device: int = 0):
-    """Set each Spec.variant from the tuned choice for its size bucket; returns the specs."""
+def apply(specs, dtype=np.complex64, device: int = 0, mode: str = "batch"):
+    """Set each Spec.variant from the tuned choice for its size bucket; returns the choices."""
     memo = {}
     for s in specs:
         k = (s.dim, s.order, bucket(s.n))
         if k not in memo:
-            memo[k] = tune(s.dim, s.n, s.order, dtype=dtype, device=device)
+            memo[k] = tune(s.dim, s.n, s.order, dtype=dtype, device=device, mode=mode)
         s.variant = memo[k]
-    return specs
+    return {f"{d}d/o{o}/n<={b}": v for (d, o, b), v in sorted(memo.items())}
