@@ -414,11 +414,12 @@ __global__ void __launch_bounds__(256) rhs_2d(int n, const void* __restrict__ u_
 //   TILE_64x64W  : 64 x 64,  16 strips of 4 rows (1024 threads)
 //   TILE_128x32W : 128 x 32, 8 strips of 4 rows  (1024 threads)
 //   TILE_64xO64  : 64 x (64 + 8K), 8 strips (512 threads): output tiles exactly 64 rows high
+//   TILE_64xO64M : the same region with 12 (K = 1) or 10 (K = 2) strips (768 / 640 threads)
 int tile_region_x(int shape) {
   switch (shape) {
     case TILE_64x64: return 64; case TILE_128x32: return 128; case TILE_32x32: return 32;
     case TILE_64x64W: return 64; case TILE_128x32W: return 128;
-    case TILE_64xO64: return 64;
+    case TILE_64xO64: return 64; case TILE_64xO64M: return 64;
   }
   return 0;
 }
@@ -426,7 +427,7 @@ int tile_region_y(int shape, int K) {
   switch (shape) {
     case TILE_64x64: return 64; case TILE_128x32: return 32; case TILE_32x32: return 32;
     case TILE_64x64W: return 64; case TILE_128x32W: return 32;
-    case TILE_64xO64: return 64 + 8 * K;
+    case TILE_64xO64: return 64 + 8 * K; case TILE_64xO64M: return 64 + 8 * K;
   }
   return 0;
 }
@@ -435,7 +436,7 @@ int tile_out_y(int shape, int K) { return tile_region_y(shape, K) - 8 * K; }
 bool tile_supported(int shape, int dtype) {
   if (shape == TILE_32x32) return true;
   if (shape == TILE_64x64 || shape == TILE_128x32 || shape == TILE_64x64W || shape == TILE_128x32W ||
-      shape == TILE_64xO64)
+      shape == TILE_64xO64 || shape == TILE_64xO64M)
     return dtype == NLS_C64;
   return false;
 }
@@ -486,6 +487,7 @@ static int occ_ft() {
     case TILE_64x64W: return CALL<T, K, 64, 64, 16>(__VA_ARGS__);          \
     case TILE_128x32W: return CALL<T, K, 128, 32, 8>(__VA_ARGS__);         \
     case TILE_64xO64: return CALL<T, K, 64, 64 + 8 * K, 8>(__VA_ARGS__);   \
+    case TILE_64xO64M: return CALL<T, K, 64, 64 + 8 * K, (K == 1 ? 12 : 10)>(__VA_ARGS__); \
   }
 
 int fused_2d_blocks_per_sm(int dtype, int K, int shape) {

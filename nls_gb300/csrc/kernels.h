@@ -35,6 +35,7 @@ enum TileShape2D {
   TILE_64x64W = 4,    // region 64 x 64, 1024 threads (single precision)
   TILE_128x32W = 5,   // region 128 x 32, 1024 threads (single precision)
   TILE_64xO64 = 6,    // region 64 x (64 + 8K): output tiles 64 rows high, 512 threads
+  TILE_64xO64M = 7,   // the same region with 768 (K = 1) or 640 (K = 2) threads
 };
 int tile_region_x(int shape);
 int tile_region_y(int shape, int K);
