@@ -239,6 +239,167 @@ __global__ void __launch_bounds__(512) rk4_1d_resident(const Inst1D* __restrict_
   if (cl > 1) cluster.sync();
 }
 
+// Cluster form with temporal blocking: each CTA also evaluates a halo of H = 4K nodes on both
+// sides of its segment, so the four stages of a step need only CTA-local barriers; the cluster
+// meets once per RK4 step, after every CTA has pushed the H new edge values of its segment into
+// its neighbours' state buffers (double-buffered by step parity, so a push never lands in a
+// buffer a neighbour is still reading).  Nodes outside [0, n) are never evaluated and stay zero.
+template <typename T, int K, int NPT>
+__global__ void __launch_bounds__(512) rk4_1d_cluster_tb(const Inst1D* __restrict__ insts, int cl,
+                                                         int seg_cap) {
+  typedef typename C2<T>::type C;
+  constexpr int H = 4 * K;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int inst = blockIdx.x / cl;
+  const int rank = blockIdx.x % cl;
+  const Inst1D& I = insts[inst];
+  const int n = I.n;
+  const int seg = (n + cl - 1) / cl;
+  const int p0 = rank * seg;
+  const int len = max(0, min(seg, n - p0));
+  const int NT = blockDim.x;
+  const int tid = threadIdx.x;
+  const int W = seg_cap + 2 * H;
+  // buffers: state A[0], A[1] (by step parity), stage buffers B0, B1; element li lives at li + H
+  C* A[2] = {reinterpret_cast<C*>(smem_raw) + H, reinterpret_cast<C*>(smem_raw) + W + H};
+  C* B0 = reinterpret_cast<C*>(smem_raw) + 2 * W + H;
+  C* B1 = reinterpret_cast<C*>(smem_raw) + 3 * W + H;
+  cg::cluster_group cluster = cg::this_cluster();
+  C* leftA[2] = {nullptr, nullptr};
+  C* rightA[2] = {nullptr, nullptr};
+  if (rank > 0) {
+    leftA[0] = cluster.map_shared_rank(A[0], rank - 1);
+    leftA[1] = cluster.map_shared_rank(A[1], rank - 1);
+  }
+  if (rank < cl - 1) {
+    rightA[0] = cluster.map_shared_rank(A[0], rank + 1);
+    rightA[1] = cluster.map_shared_rank(A[1], rank + 1);
+  }
+  C* base = reinterpret_cast<C*>(smem_raw);
+  for (int i = tid; i < 4 * W; i += NT) base[i] = mk<T>(0, 0);
+  __syncthreads();
+
+  const Params<T>& prm = ParamsOf<T>::get(I);
+  const Phys<T> ph = phys_of<T>(prm);
+  const RK<T> rk = rk_of<T>(prm);
+  const Weights1D<T, K> w = load_w<T, K>(I.op);
+  const T h = (T)I.op.h;
+  const C* __restrict__ Ug = reinterpret_cast<const C*>(I.u);
+  const T* __restrict__ Pg = reinterpret_cast<const T*>(I.P);
+
+  // owned local indices li = tid + j*NT - H, j < NPT, covering [-H, seg + H)
+  C u[NPT], acc[NPT];
+  T pc[NPT], ir[NPT];
+  unsigned indom = 0;
+#pragma unroll
+  for (int j = 0; j < NPT; ++j) {
+    const int li = tid + j * NT - H;
+    const int p = p0 + li;
+    const bool in = li < seg + H && p >= 0 && p < n;
+    indom |= (unsigned)in << j;
+    u[j] = in ? Ug[p] : mk<T>(0, 0);
+    pc[j] = in ? ph.c12 * Pg[p] : (T)0;
+    ir[j] = (in && p >= K) ? (T)1 / ((T)p * h) : (T)0;
+    acc[j] = mk<T>(0, 0);
+    if (in) A[0][li] = u[j];
+  }
+  __syncthreads();
+
+  auto lap = [&](const C* in, int li, int p, T irv) -> C {
+    C lu;
+    if (p >= K) {
+      T d2x = 0, d2y = 0, d1x = 0, d1y = 0;
+#pragma unroll
+      for (int d = -K; d <= K; ++d) {
+        const C v = in[li + d];
+        d2x += w.w2[d + K] * v.x;
+        d2y += w.w2[d + K] * v.y;
+        if (d != 0) {
+          d1x += w.w1[d + K] * v.x;
+          d1y += w.w1[d + K] * v.y;
+        }
+      }
+      lu.x = d2x + irv * d1x;
+      lu.y = d2y + irv * d1y;
+    } else {
+      T lx = 0, ly = 0;
+#pragma unroll
+      for (int d = -K; d <= K; ++d) {
+        const T a = ParamsOf<T>::near(I.op, p, d + K);
+        lx += a * in[li + d].x;
+        ly += a * in[li + d].y;
+      }
+      lu.x = lx;
+      lu.y = ly;
+    }
+    return lu;
+  };
+  auto kval = [&](C v, T pcv, C lu) -> C {
+    const T sq = v.x * v.x + v.y * v.y;
+    const T r = rdiv(pcv, ph.c13 + ph.c14 * sq);
+    const T a = ph.c3 * r - ph.c4;
+    const T b = ph.c5 * sq + ph.c6 * r;
+    C k;
+    k.x = a * v.x + b * v.y - lu.y;
+    k.y = a * v.y - b * v.x + lu.x;
+    return k;
+  };
+
+  const int64_t steps = I.steps;
+  for (int64_t step = 0; step < steps; ++step) {
+    const int par = (int)(step & 1);
+    C* Acur = A[par];
+    C* Anext = A[par ^ 1];
+    // halo values pushed by the neighbours at the end of the previous step
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) {
+      const int li = tid + j * NT - H;
+      if ((indom >> j) & 1u) u[j] = Acur[li];
+    }
+#pragma unroll 1
+    for (int s = 1; s <= 4; ++s) {
+      const C* in = s == 1 ? Acur : (s == 3 ? B1 : B0);
+      C* out = s == 2 ? B1 : B0;
+      const int lo = s < 4 ? -(H - s * K) : 0;
+      const int hi = s < 4 ? seg + H - s * K : len;
+      const T coef = s == 3 ? rk.dt : rk.half_dt;
+      const T wk = (s == 2 || s == 3) ? (T)2 : (T)1;
+#pragma unroll
+      for (int j = 0; j < NPT; ++j) {
+        const int li = tid + j * NT - H;
+        if (((indom >> j) & 1u) && li >= lo && li < hi) {
+          const int p = p0 + li;
+          const C k = kval(in[li], pc[j], lap(in, li, p, ir[j]));
+          if (s == 1) acc[j] = k;
+          else {
+            acc[j].x += wk * k.x;
+            acc[j].y += wk * k.y;
+          }
+          if (s < 4) {
+            out[li] = mk<T>(u[j].x + coef * k.x, u[j].y + coef * k.y);
+          } else {
+            const C un = mk<T>(u[j].x + rk.dt6 * acc[j].x, u[j].y + rk.dt6 * acc[j].y);
+            u[j] = un;
+            Anext[li] = un;
+            if (leftA[0] && li < H) leftA[par ^ 1][seg + li] = un;
+            if (rightA[0] && li >= seg - H) rightA[par ^ 1][li - seg] = un;
+          }
+        }
+      }
+      if (s < 4) __syncthreads();
+    }
+    cluster.sync();
+  }
+
+  C* __restrict__ Uo = reinterpret_cast<C*>(I.u);
+#pragma unroll
+  for (int j = 0; j < NPT; ++j) {
+    const int li = tid + j * NT - H;
+    if (((indom >> j) & 1u) && li >= 0 && li < len) Uo[p0 + li] = u[j];
+  }
+  cluster.sync();
+}
+
 // One RK4 stage of a 1-D grid held in global memory (see nls_common.cuh for the stage scheme).
 template <typename T, int K>
 __global__ void __launch_bounds__(256) rk4_1d_stage(int n, int s, const void* __restrict__ src_,
@@ -311,16 +472,20 @@ __global__ void __launch_bounds__(256) rhs_1d(int n, const void* __restrict__ u_
 template <typename T, int K, int NPT>
 static cudaError_t launch_res(const Inst1D* d_insts, int count, int cl, int seg_cap, int nt,
                               cudaStream_t stream, bool prepare_only) {
-  auto kern = rk4_1d_resident<T, K, NPT>;
-  const size_t smem = (size_t)2 * (seg_cap + 2 * K) * sizeof(typename C2<T>::type);
+  // one CTA: per-stage CTA barriers; a cluster: the temporally blocked form (one cluster
+  // barrier per step)
+  auto kern = cl > 1 ? rk4_1d_cluster_tb<T, K, NPT> : rk4_1d_resident<T, K, NPT>;
+  const size_t smem = cl > 1 ? (size_t)4 * (seg_cap + 8 * K) * sizeof(typename C2<T>::type)
+                             : (size_t)2 * (seg_cap + 2 * K) * sizeof(typename C2<T>::type);
   // Attributes are raised once, monotonically, so launches inside a stream capture never need
   // to change them (prepare_1d_resident runs before any capture).
-  static size_t configured_smem = 0;
+  static size_t configured_smem[2] = {0, 0};
   static bool non_portable = false;
-  if (smem > configured_smem) {
+  const int ki = cl > 1 ? 1 : 0;
+  if (smem > configured_smem[ki]) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    configured_smem = smem;
+    configured_smem[ki] = smem;
   }
   if (cl > 8 && !non_portable) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -346,10 +511,12 @@ static cudaError_t launch_res(const Inst1D* d_insts, int count, int cl, int seg_
 template <typename T, int K>
 static cudaError_t launch_res_npt(const Inst1D* d, int count, int cl, int seg_cap, cudaStream_t s,
                                   bool prepare_only) {
-  // threads: up to 512; nodes per thread: 1, 2, 4 or 8 (8 only in single precision)
+  // threads: up to 512; nodes per thread: 1, 2, 4 or 8 (8 only in single precision); the
+  // cluster form also owns a halo of 4K nodes on each side
+  const int nodes = cl > 1 ? seg_cap + 8 * K : seg_cap;
   int npt = 1;
-  while (npt * 512 < seg_cap) npt *= 2;
-  int nt = (seg_cap + npt - 1) / npt;
+  while (npt * 512 < nodes) npt *= 2;
+  int nt = (nodes + npt - 1) / npt;
   nt = ((nt + 31) / 32) * 32;
   if (nt > 512) nt = 512;
   switch (npt) {

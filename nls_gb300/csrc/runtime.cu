@@ -134,7 +134,9 @@ static int choose_cl(int dtype, int n, int K, int variant) {
   auto feasible = [&](int cl) {
     if (cl < 1 || cl > 16) return false;
     const int seg = (n + cl - 1) / cl;
-    return seg <= lim && seg >= 2 * K;
+    if (cl == 1) return seg <= lim && seg >= 2 * K;
+    // the cluster form keeps 4 buffers of seg + 8K nodes and needs segments of at least 4K
+    return seg + 8 * K <= lim && seg >= 4 * K;
   };
   if (variant == 0) return 0;
   if (variant > 0) return feasible(variant) ? variant : -1;
@@ -782,6 +784,28 @@ NLS_API int nls_make_laplacian_2d(int n, int order, double h, double* blocks, in
   return host_make_laplacian_2d(n, order, h, blocks, orders);
 }
 
+static void ctx_release(nls_ctx* ctx) {
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->aux) cudaStreamSynchronize(ctx->aux);
+  for (int i = 0; i < nls_ctx::kSide; ++i)
+    if (ctx->side[i]) cudaStreamSynchronize(ctx->side[i]);
+  ctx->scratch.release();
+  ctx->desc.release();
+  ctx->io.release();
+  ctx->diag.release();
+  ctx->diagv.release();
+  if (ctx->h_diag) cudaFreeHost(ctx->h_diag);
+  for (int i = 0; i < nls_ctx::kSide; ++i) {
+    if (ctx->side_done[i]) cudaEventDestroy(ctx->side_done[i]);
+    if (ctx->side[i]) cudaStreamDestroy(ctx->side[i]);
+  }
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->aux) cudaStreamDestroy(ctx->aux);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
 NLS_API int nls_ctx_create(int device, nls_ctx** out) {
   if (!out) return NLS_ERR_INVALID;
   *out = nullptr;
@@ -791,21 +815,18 @@ NLS_API int nls_ctx_create(int device, nls_ctx** out) {
   if (device < 0 || device >= ndev) return NLS_ERR_INVALID;
   nls_ctx* ctx = new nls_ctx();
   ctx->device = device;
-  if ((e = cudaSetDevice(device)) != cudaSuccess ||
-      (e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming)) != cudaSuccess) {
-    delete ctx;
+  bool ok = cudaSetDevice(device) == cudaSuccess &&
+            cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; ok && i < nls_ctx::kSide; ++i)
+    ok = cudaStreamCreateWithFlags(&ctx->side[i], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&ctx->side_done[i], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    ctx_release(ctx);
     return NLS_ERR_CUDA;
-  }
-  for (int i = 0; i < nls_ctx::kSide; ++i) {
-    if (cudaStreamCreateWithFlags(&ctx->side[i], cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->side_done[i], cudaEventDisableTiming) != cudaSuccess) {
-      delete ctx;
-      return NLS_ERR_CUDA;
-    }
   }
   *out = ctx;
   return NLS_OK;
@@ -814,24 +835,7 @@ NLS_API int nls_ctx_create(int device, nls_ctx** out) {
 NLS_API int nls_ctx_destroy(nls_ctx* ctx) {
   if (!ctx) return NLS_ERR_INVALID;
   cudaSetDevice(ctx->device);
-  cudaStreamSynchronize(ctx->stream);
-  cudaStreamSynchronize(ctx->aux);
-  ctx->scratch.release();
-  ctx->desc.release();
-  ctx->io.release();
-  ctx->diag.release();
-  ctx->diagv.release();
-  if (ctx->h_diag) cudaFreeHost(ctx->h_diag);
-  cudaEventDestroy(ctx->ev_fork);
-  cudaEventDestroy(ctx->ev_join);
-  for (int i = 0; i < nls_ctx::kSide; ++i) {
-    cudaStreamSynchronize(ctx->side[i]);
-    cudaEventDestroy(ctx->side_done[i]);
-    cudaStreamDestroy(ctx->side[i]);
-  }
-  cudaStreamDestroy(ctx->aux);
-  cudaStreamDestroy(ctx->stream);
-  delete ctx;
+  ctx_release(ctx);
   return NLS_OK;
 }
 
@@ -994,6 +998,12 @@ NLS_API int nls_batch_run(nls_batch* b, int64_t steps) {
   int st = batch_descriptors(b, steps);
   if (st) return st;
   auto it = b->graphs.find(steps);
+  if (it == b->graphs.end() && b->graphs.size() >= 8) {
+    // keep the cache small: a caller cycling through step counts re-captures instead of growing it
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+  }
   if (it == b->graphs.end()) {
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;

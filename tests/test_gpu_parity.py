@@ -149,7 +149,7 @@ def test_1d_c64_vs_oracles(gpu, oracle_lib, order, variant):
 
 
 @pytest.mark.parametrize("order", [3, 5])
-@pytest.mark.parametrize("variant", [-1, 0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [-1, 0, 1, 2, 3, 4, 5, 6, 7])
 def test_2d_c64_vs_oracles(gpu, oracle_lib, order, variant):
     s = _spec_2d(150, order)
     iters = 400
