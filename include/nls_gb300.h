@@ -48,7 +48,9 @@ typedef struct nls_pool nls_pool;
  * the autotuner (-1 = built-in choice): 1-D = CTAs per solve (cluster size 1..16, 0 = unfused
  * stage kernels); 2-D = 0 unfused, or a fused tile region (threads): 1 = 64x64 (512),
  * 2 = 128x32 (512), 3 = 32x32 (256), 4 = 64x64 (1024), 5 = 128x32 (1024),
- * 6 = 64 x (64 + 8K) with output tiles exactly 64 rows high (512). */
+ * 6 = 64 x (64 + 8K) with output tiles exactly 64 rows high (512), 7 = the same region with 768
+ * (order 3) or 640 (order 5) threads; register-resident tiles (complex64 only), region 64 wide:
+ * 8 = 64x80 (512), 9 = 64x96 (384), 10 = 64x96 (256), 11 = 64x64 (512). */
 typedef struct nls_problem {
   int dim;
   int n;

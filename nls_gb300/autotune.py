@@ -43,7 +43,7 @@ def bucket(n: int) -> int:
 def candidates(dim: int, dtype, n: int):
     c64 = np.dtype(dtype) == np.dtype(np.complex64)
     if dim == 2:
-        return [6, 1, 7, 2, 3, 4, 5, 0] if c64 else [0, 3]
+        return [10, 9, 8, 11, 6, 1, 7, 2, 3, 4, 5, 0] if c64 else [0, 3]
     out = []
     lim = 4096 if c64 else 2048
     for cl in (1, 2, 4, 8, 16):

@@ -191,6 +191,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+}  // namespace nlsg
+
+#include "k2d_reg.cuh"
+
+namespace nlsg {
+
 template <typename T, int K, int RX, int RY, int NS, bool TMA>
 __global__ void __launch_bounds__(TileCfg<T, K, RX, RY, NS>::NT, TileCfg<T, K, RX, RY, NS>::MINB)
 rk4_2d_fused(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items, int n_items,
@@ -415,11 +421,13 @@ __global__ void __launch_bounds__(256) rhs_2d(int n, const void* __restrict__ u_
 //   TILE_128x32W : 128 x 32, 8 strips of 4 rows  (1024 threads)
 //   TILE_64xO64  : 64 x (64 + 8K), 8 strips (512 threads): output tiles exactly 64 rows high
 //   TILE_64xO64M : the same region with 12 (K = 1) or 10 (K = 2) strips (768 / 640 threads)
+//   TILE_R64x*   : rk4_2d_reg, region 64 x (warps x rows per warp), see k2d_reg.cuh
 int tile_region_x(int shape) {
   switch (shape) {
     case TILE_64x64: return 64; case TILE_128x32: return 128; case TILE_32x32: return 32;
     case TILE_64x64W: return 64; case TILE_128x32W: return 128;
     case TILE_64xO64: return 64; case TILE_64xO64M: return 64;
+    case TILE_R64x80: case TILE_R64x96: case TILE_R64x96S: case TILE_R64x64: return 64;
   }
   return 0;
 }
@@ -428,15 +436,20 @@ int tile_region_y(int shape, int K) {
     case TILE_64x64: return 64; case TILE_128x32: return 32; case TILE_32x32: return 32;
     case TILE_64x64W: return 64; case TILE_128x32W: return 32;
     case TILE_64xO64: return 64 + 8 * K; case TILE_64xO64M: return 64 + 8 * K;
+    case TILE_R64x80: return 80; case TILE_R64x96: return 96; case TILE_R64x96S: return 96;
+    case TILE_R64x64: return 64;
   }
   return 0;
+}
+static bool reg_shape(int shape) {
+  return shape == TILE_R64x80 || shape == TILE_R64x96 || shape == TILE_R64x96S || shape == TILE_R64x64;
 }
 int tile_out_x(int shape, int K) { return tile_region_x(shape) - 8 * K; }
 int tile_out_y(int shape, int K) { return tile_region_y(shape, K) - 8 * K; }
 bool tile_supported(int shape, int dtype) {
   if (shape == TILE_32x32) return true;
   if (shape == TILE_64x64 || shape == TILE_128x32 || shape == TILE_64x64W || shape == TILE_128x32W ||
-      shape == TILE_64xO64 || shape == TILE_64xO64M)
+      shape == TILE_64xO64 || shape == TILE_64xO64M || reg_shape(shape))
     return dtype == NLS_C64;
   return false;
 }
@@ -479,6 +492,33 @@ static int occ_ft() {
   return occ_f<T, K, RX, RY, NS, true>();
 }
 
+template <int K, int NW, int NJ, bool TMA>
+static cudaError_t launch_r(const Inst2D* d_insts, const TileItem* d_items, int n_items, int j_step,
+                            int grid, cudaStream_t s) {
+  typedef RegCfg<K, NW, NJ> G;
+  rk4_2d_reg<K, NW, NJ, TMA><<<grid, G::NT, G::SMEM, s>>>(d_insts, d_items, n_items, j_step);
+  return cudaGetLastError();
+}
+// Sets the shared-memory attribute (outside any capture) and returns CTAs per SM.
+template <int K, int NW, int NJ, bool TMA>
+static int occ_r() {
+  typedef RegCfg<K, NW, NJ> G;
+  auto kern = rk4_2d_reg<K, NW, NJ, TMA>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM) != cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, G::NT, G::SMEM) != cudaSuccess) return 0;
+  return nb;
+}
+
+#define NLSG_REG_SHAPES(K, TMA, CALL, ...)                                 \
+  switch (shape) {                                                         \
+    case TILE_R64x80: return CALL<K, 16, 5, TMA>(__VA_ARGS__);             \
+    case TILE_R64x96: return CALL<K, 12, 8, TMA>(__VA_ARGS__);             \
+    case TILE_R64x96S: return CALL<K, 8, 12, TMA>(__VA_ARGS__);            \
+    case TILE_R64x64: return CALL<K, 16, 4, TMA>(__VA_ARGS__);             \
+  }
+
 #define NLSG_SHAPES(T, K, CALL, ...)                                        \
   switch (shape) {                                                         \
     case TILE_64x64: return CALL<T, K, 64, 64, 8>(__VA_ARGS__);            \
@@ -498,6 +538,11 @@ int fused_2d_blocks_per_sm(int dtype, int K, int shape) {
     if (K == 2) return occ_f<double, 2, 32, 32, 8>();
     return 0;
   }
+  if (reg_shape(shape)) {
+    if (K == 1) { NLSG_REG_SHAPES(1, false, occ_r) }
+    if (K == 2) { NLSG_REG_SHAPES(2, false, occ_r) }
+    return 0;
+  }
   if (K == 1) { NLSG_SHAPES(float, 1, occ_f) }
   if (K == 2) { NLSG_SHAPES(float, 2, occ_f) }
   return 0;
@@ -514,6 +559,11 @@ cudaError_t launch_2d_fused(int dtype, int K, int shape, const Inst2D* d_insts,
     if (K == 2) return launch_f<double, 2, 32, 32, 8>(d_insts, d_items, n_items, j_step, grid, s);
     return cudaErrorInvalidValue;
   }
+  if (reg_shape(shape)) {
+    if (K == 1) { NLSG_REG_SHAPES(1, false, launch_r, d_insts, d_items, n_items, j_step, grid, s) }
+    if (K == 2) { NLSG_REG_SHAPES(2, false, launch_r, d_insts, d_items, n_items, j_step, grid, s) }
+    return cudaErrorInvalidValue;
+  }
   if (K == 1) { NLSG_SHAPES(float, 1, launch_f, d_insts, d_items, n_items, j_step, grid, s) }
   if (K == 2) { NLSG_SHAPES(float, 2, launch_f, d_insts, d_items, n_items, j_step, grid, s) }
   return cudaErrorInvalidValue;
@@ -523,6 +573,11 @@ cudaError_t launch_2d_fused(int dtype, int K, int shape, const Inst2D* d_insts,
 
 int fused_2d_tma_blocks_per_sm(int K, int shape) {
   if (!tile_supported(shape, NLS_C64)) return 0;
+  if (reg_shape(shape)) {
+    if (K == 1) { NLSG_REG_SHAPES(1, true, occ_r) }
+    if (K == 2) { NLSG_REG_SHAPES(2, true, occ_r) }
+    return 0;
+  }
   if (K == 1) { NLSG_SHAPES(float, 1, occ_ft) }
   if (K == 2) { NLSG_SHAPES(float, 2, occ_ft) }
   return 0;
@@ -532,6 +587,11 @@ cudaError_t launch_2d_fused_tma(int K, int shape, const Inst2D* d_insts, const T
                                 int n_items, int j_step, int grid, cudaStream_t s) {
   if (n_items <= 0) return cudaSuccess;
   if (!tile_supported(shape, NLS_C64)) return cudaErrorInvalidValue;
+  if (reg_shape(shape)) {
+    if (K == 1) { NLSG_REG_SHAPES(1, true, launch_r, d_insts, d_items, n_items, j_step, grid, s) }
+    if (K == 2) { NLSG_REG_SHAPES(2, true, launch_r, d_insts, d_items, n_items, j_step, grid, s) }
+    return cudaErrorInvalidValue;
+  }
   if (K == 1) { NLSG_SHAPES(float, 1, launch_ft, d_insts, d_items, n_items, j_step, grid, s) }
   if (K == 2) { NLSG_SHAPES(float, 2, launch_ft, d_insts, d_items, n_items, j_step, grid, s) }
   return cudaErrorInvalidValue;

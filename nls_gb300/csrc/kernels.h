@@ -36,6 +36,11 @@ enum TileShape2D {
   TILE_128x32W = 5,   // region 128 x 32, 1024 threads (single precision)
   TILE_64xO64 = 6,    // region 64 x (64 + 8K): output tiles 64 rows high, 512 threads
   TILE_64xO64M = 7,   // the same region with 768 (K = 1) or 640 (K = 2) threads
+  // register-resident tiles (rk4_2d_reg, single precision): region 64 wide, warp = row strip
+  TILE_R64x80 = 8,    // 16 warps x 5 rows (512 threads)
+  TILE_R64x96 = 9,    // 12 warps x 8 rows (384 threads)
+  TILE_R64x96S = 10,  // 8 warps x 12 rows (256 threads)
+  TILE_R64x64 = 11,   // 16 warps x 4 rows (512 threads)
 };
 int tile_region_x(int shape);
 int tile_region_y(int shape, int K);
