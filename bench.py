@@ -45,9 +45,21 @@ def _peaks():
     return 6800.0, "fallback"
 
 
+# 2-D fused-step kernel of each tile shape (the C ABI's 2-D variant numbers)
+SHAPE_KERNELS = {
+    1: "rk4_2d_fused 64x64 region, 512 threads", 2: "rk4_2d_fused 128x32, 512 threads",
+    3: "rk4_2d_fused 32x32, 256 threads", 4: "rk4_2d_fused 64x64, 1024 threads",
+    5: "rk4_2d_fused 128x32, 1024 threads", 6: "rk4_2d_fused 64x(64+8K), 512 threads",
+    7: "rk4_2d_fused 64x(64+8K), 768/640 threads", 8: "rk4_2d_reg 64x80, 16 warps x 5 rows",
+    9: "rk4_2d_reg 64x96, 12 warps x 8 rows", 10: "rk4_2d_reg 64x96, 8 warps x 12 rows",
+    11: "rk4_2d_reg 64x64, 16 warps x 4 rows",
+}
+DEFAULT_SHAPE_C64 = 10
+
+
 def _traffic_per_node():
     """DRAM bytes per node per fused-step launch from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "rk4_2d_fused_c64_batch_mix.md")
+    p = os.path.join(ROOT, "profiles", "rk4_2d_reg_c64_batch_mix.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -404,7 +416,9 @@ def run_ours(args):
     tpn = _traffic_per_node()
     result["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                           "frac": achieved / peak, "traffic": (tpn * nodes_2d if tpn else None),
-                          "kernel": "rk4_2d_fused<float,K=1,64x72,TMA> over all 2-D tiles, one launch per RK4 step",
+                          "kernel": "; ".join(sorted({SHAPE_KERNELS.get(v if v > 0 else DEFAULT_SHAPE_C64, str(v))
+                                                      for v in (sp.variant for sp in specs2)}))
+                                    + " (TMA prefetch); one launch per RK4 step over all 2-D tiles",
                           "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": launch_s * 1e6,
                           "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"}
     b2.close()

@@ -30,9 +30,32 @@ struct RegCfg {
   static constexpr size_t STAGE_U = (size_t)RX * RY * 8;            // complex64 state box
   static constexpr size_t STAGE_P = (size_t)RX * RY * 4;            // pump box
   static constexpr size_t EXCH = (size_t)2 * NW * 2 * K * RX * 8;   // strip-end rows, 2 parities
-  static constexpr size_t SMEM = STAGE_U + STAGE_P + EXCH + 16;     // + the TMA mbarrier
+  static constexpr size_t DESC = sizeof(Inst2D);                   // descriptor copy (TMA path)
+  static constexpr size_t OFF_DESC = STAGE_U + STAGE_P + EXCH;      // two descriptor slots
+  static constexpr size_t OFF_CTRL = OFF_DESC + 2 * DESC;
+  static constexpr size_t SMEM = OFF_CTRL + 128;                    // + control block
   static_assert(NJ >= K && NJ <= 32 && TY > 0, "tile layout");
+  static_assert(DESC % 16 == 0, "a descriptor bulk copy moves a multiple of 16 bytes");
 };
+
+// Control block of the TMA path in shared memory.  Slot b (b = tile count & 1) names the work
+// item whose boxes and descriptor the current or the next copy brings; the cand* fields are
+// filled by the elected thread's asynchronous lookups of the item after that.
+struct RegCtrl {
+  uint64_t bar;               // transaction barrier of the boxes and the descriptor
+  int item[2];                // work-list index of slot b (>= n_items: none)
+  TileItem ti[2];
+  int nx_idx;                 // next item to issue (elected thread)
+  TileItem nx_ti;
+  int nx_tiles_x, nx_parity;
+  const void* nx_tmap;
+  int cand_idx, slot;         // candidate after the next item; slot of the current tile
+  TileItem cand_ti;           // asynchronous lookups (cp.async) of the candidate after that
+  long long cand_steps;
+  int cand_tiles_x, cand_parity;
+  const void* cand_tmap;
+};
+static_assert(sizeof(RegCtrl) <= 128, "control block");
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
@@ -46,6 +69,24 @@ __device__ __forceinline__ float rcp_approx(float x) {
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
+
+// Untiled bulk copy global -> shared, completing on the transaction barrier.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+// Small asynchronous global -> shared copies (cp.async), so a lookup's latency is not waited on
+// until its result is needed.
+template <int BYTES>
+__device__ __forceinline__ void async_copy(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_u32(dst)),
+               "l"(reinterpret_cast<uint64_t>(src)), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void async_commit_wait() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_all;" ::: "memory");
+}
+__device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 
 // Per-tile constants as broadcast pairs (both halves equal) for the packed pipe.  The stage
 // slopes are carried pre-multiplied by dt/2 (q = dt/2 * k), so the weights and coefficients of
@@ -177,10 +218,11 @@ __device__ __forceinline__ void reg_stage(float2 (&tX)[NJ], float2 (&tY)[NJ], fl
   }
 }
 
-template <int K, int NW, int NJ, bool EDGE>
+// The four stages of a step; mid() runs between the second and the third.
+template <int K, int NW, int NJ, bool EDGE, typename Mid>
 __device__ __forceinline__ void reg_step(float2 (&uX)[NJ], float2 (&uY)[NJ], const float2 (&pc)[NJ],
                                          unsigned dom0, unsigned dom1, float4* __restrict__ exch,
-                                         int warp, int lane, const RegConst& c) {
+                                         int warp, int lane, const RegConst& c, Mid&& mid) {
   float2 tX[NJ], tY[NJ], aX[NJ], aY[NJ];
 #pragma unroll
   for (int j = 0; j < NJ; ++j) {
@@ -189,6 +231,7 @@ __device__ __forceinline__ void reg_step(float2 (&uX)[NJ], float2 (&uY)[NJ], con
   }
   reg_stage<K, NW, NJ, 1, EDGE>(tX, tY, aX, aY, uX, uY, pc, dom0, dom1, exch, warp, lane, c);
   reg_stage<K, NW, NJ, 2, EDGE>(tX, tY, aX, aY, uX, uY, pc, dom0, dom1, exch, warp, lane, c);
+  mid();
   reg_stage<K, NW, NJ, 3, EDGE>(tX, tY, aX, aY, uX, uY, pc, dom0, dom1, exch, warp, lane, c);
   reg_stage<K, NW, NJ, 4, EDGE>(tX, tY, aX, aY, uX, uY, pc, dom0, dom1, exch, warp, lane, c);
 }
@@ -202,48 +245,15 @@ rk4_2d_reg(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items,
   float4* stage_u = reinterpret_cast<float4*>(smem_raw);                   // [RY][32] node pairs
   float2* stage_p = reinterpret_cast<float2*>(smem_raw + G::STAGE_U);      // [RY][32]
   float4* exch = reinterpret_cast<float4*>(smem_raw + G::STAGE_U + G::STAGE_P);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + G::STAGE_U + G::STAGE_P + G::EXCH);
+  Inst2D* desc = reinterpret_cast<Inst2D*>(smem_raw + G::OFF_DESC);       // [2]
+  RegCtrl* ctrl = reinterpret_cast<RegCtrl*>(smem_raw + G::OFF_CTRL);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int x0 = 2 * lane;  // region column of the pair's first node
   const int y0 = warp * NJ;
 
-  auto active = [&](int idx) -> bool {
-    return idx < n_items && (int64_t)j_step < insts[items[idx].inst].steps;
-  };
-  auto issue = [&](int idx) {
-    const TileItem ti = items[idx];
-    const Inst2D& I = insts[ti.inst];
-    const int tyi = ti.tile / I.tiles_x;
-    const int txi = ti.tile - tyi * I.tiles_x;
-    const int par = (I.parity + j_step) & 1;
-    const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(I.tmap);
-    fence_proxy_async_smem();
-    mbar_expect_tx(bar, (uint32_t)(G::STAGE_U + G::STAGE_P));
-    tma_load_2d(stage_u, maps + par, txi * G::TX - H, tyi * G::TY - H, bar);
-    tma_load_2d(stage_p, maps + 2, txi * G::TX - H, tyi * G::TY - H, bar);
-  };
-  uint32_t phase = 0;
-  int it = blockIdx.x;
-  if (TMA) {
-    if (threadIdx.x == 0) {
-      mbar_init(bar, 1);
-      fence_mbar_init();
-    }
-    __syncthreads();
-    while (it < n_items && !active(it)) it += gridDim.x;
-    if (threadIdx.x == 0 && it < n_items) issue(it);
-  }
-
-  while (it < n_items) {
-    const TileItem ti = items[it];
-    const Inst2D& I = insts[ti.inst];
-    int nxt = it + gridDim.x;
-    if (TMA) {
-      while (nxt < n_items && !active(nxt)) nxt += gridDim.x;
-    } else if ((int64_t)j_step >= I.steps) {
-      it = nxt;
-      continue;
-    }
+  // One tile: load this thread's rows (from the staging boxes or from global memory), run the
+  // step, store the output rows.
+  auto run_tile = [&](const Inst2D& I, TileItem ti, auto&& boxes_read, auto&& mid) {
     const int n = I.n;
     const int par = (I.parity + j_step) & 1;
     const float2* __restrict__ src = reinterpret_cast<const float2*>(I.u[par]);
@@ -258,19 +268,6 @@ rk4_2d_reg(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items,
     const Params<float>& prm = I.pf;
     const RegConst c = reg_const(prm);
     const float2 c12 = f2(prm.c12, prm.c12);
-
-    if (TMA) {
-      bool ok = true;
-      if (threadIdx.x == 0) ok = mbar_wait(bar, phase);
-      if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) {
-          atomicExch(&g_tile_wait_timeout, 1);
-          mbar_wait(bar, phase);  // let the copies in flight land before the CTA leaves
-        }
-        return;
-      }
-      phase ^= 1u;
-    }
     float2 uX[NJ], uY[NJ], pc[NJ];
     unsigned dom0 = 0, dom1 = 0;
     const bool xin0 = gx >= 0 && gx < n, xin1 = gx + 1 >= 0 && gx + 1 < n;
@@ -297,12 +294,9 @@ rk4_2d_reg(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items,
       dom0 |= (unsigned)i0 << j;
       dom1 |= (unsigned)i1 << j;
     }
-    if (TMA) {
-      __syncthreads();  // the staging boxes are free again: fetch the next tile's meanwhile
-      if (threadIdx.x == 0 && nxt < n_items) issue(nxt);
-    }
-    if (edge) reg_step<K, NW, NJ, true>(uX, uY, pc, dom0, dom1, exch, warp, lane, c);
-    else reg_step<K, NW, NJ, false>(uX, uY, pc, dom0, dom1, exch, warp, lane, c);
+    boxes_read();
+    if (edge) reg_step<K, NW, NJ, true>(uX, uY, pc, dom0, dom1, exch, warp, lane, c, mid);
+    else reg_step<K, NW, NJ, false>(uX, uY, pc, dom0, dom1, exch, warp, lane, c, mid);
     // output tile: region rows and columns [H, R - H) inside the grid
     const bool xout = x0 >= H && x0 < G::RX - H;
 #pragma unroll
@@ -320,7 +314,126 @@ rk4_2d_reg(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items,
         }
       }
     }
-    it = nxt;
+  };
+
+  if (!TMA) {
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+      const TileItem ti = items[it];
+      const Inst2D& I = insts[ti.inst];
+      if ((int64_t)j_step >= I.steps) continue;
+      run_tile(I, ti, [] {}, [] {});
+    }
+    return;
+  }
+
+  // ---- TMA path: the elected thread (thread 0) keeps one tile in flight and looks up the one
+  // after it while the current tile is computed.
+  uint64_t* bar = &ctrl->bar;
+  // synchronous scan for the first active item at idx, idx + grid, ...; result in ctrl->nx_*
+  auto scan = [&](int idx) {
+    TileItem ti = {0, 0};
+    for (; idx < n_items; idx += gridDim.x) {
+      ti = items[idx];
+      if ((int64_t)j_step < insts[ti.inst].steps) break;
+    }
+    ctrl->nx_idx = idx;
+    if (idx < n_items) {
+      const Inst2D& I = insts[ti.inst];
+      ctrl->nx_ti = ti;
+      ctrl->nx_tiles_x = I.tiles_x;
+      ctrl->nx_parity = I.parity;
+      ctrl->nx_tmap = I.tmap;
+    }
+  };
+  // copy the boxes and the descriptor of item ctrl->nx_* into slot b
+  auto issue = [&](int b) {
+    const TileItem ti = ctrl->nx_ti;
+    const int tyi = ti.tile / ctrl->nx_tiles_x;
+    const int txi = ti.tile - tyi * ctrl->nx_tiles_x;
+    const int par = (ctrl->nx_parity + j_step) & 1;
+    const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(ctrl->nx_tmap);
+    ctrl->item[b] = ctrl->nx_idx;
+    ctrl->ti[b] = ti;
+    fence_proxy_async_smem();
+    mbar_expect_tx(bar, (uint32_t)(G::STAGE_U + G::STAGE_P + G::DESC));
+    tma_load_2d(stage_u, maps + par, txi * G::TX - H, tyi * G::TY - H, bar);
+    tma_load_2d(stage_p, maps + 2, txi * G::TX - H, tyi * G::TY - H, bar);
+    bulk_load(desc + b, insts + ti.inst, (uint32_t)G::DESC, bar);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+    scan(blockIdx.x);
+    if (ctrl->nx_idx < n_items) {
+      issue(0);
+      scan(ctrl->nx_idx + gridDim.x);
+    } else {
+      ctrl->item[0] = n_items;
+    }
+  }
+  __syncthreads();
+  uint32_t phase = 0;
+  for (int b = 0;; b ^= 1) {
+    if (ctrl->item[b] >= n_items) break;
+    bool ok = true;
+    if (threadIdx.x == 0) ok = mbar_wait(bar, phase);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(&g_tile_wait_timeout, 1);
+        mbar_wait(bar, phase);  // let the copies in flight land before the CTA leaves
+      }
+      return;
+    }
+    phase ^= 1u;
+    // Hooks of the elected thread: once every thread holds its rows, fetch the next tile into
+    // the staging boxes and start the lookup of the candidate after it (work-list entry now,
+    // its descriptor fields after two stages, the decision after the step), all by cp.async so
+    // that no load is waited on while it is in flight.  Its state lives in the control block.
+    if (threadIdx.x == 0) {
+      ctrl->slot = b;
+      ctrl->cand_idx = ctrl->nx_idx < n_items ? ctrl->nx_idx + gridDim.x : n_items;
+    }
+    auto boxes_read = [&] {
+      __syncthreads();  // the staging boxes are free again
+      if (threadIdx.x != 0) return;
+      if (ctrl->nx_idx < n_items) {
+        issue(ctrl->slot ^ 1);
+        if (ctrl->cand_idx < n_items) {
+          async_copy<8>(&ctrl->cand_ti, items + ctrl->cand_idx);
+          async_commit();
+        }
+      } else {
+        ctrl->item[ctrl->slot ^ 1] = n_items;
+      }
+    };
+    auto mid = [&] {
+      if (threadIdx.x != 0 || ctrl->cand_idx >= n_items) return;
+      async_commit_wait();
+      const Inst2D* J = insts + ctrl->cand_ti.inst;
+      async_copy<8>(&ctrl->cand_steps, &J->steps);
+      async_copy<4>(&ctrl->cand_tiles_x, &J->tiles_x);
+      async_copy<4>(&ctrl->cand_parity, &J->parity);
+      async_copy<8>(&ctrl->cand_tmap, &J->tmap);
+      async_commit();
+    };
+    run_tile(desc[b], ctrl->ti[b], boxes_read, mid);
+    if (threadIdx.x == 0 && ctrl->nx_idx < n_items) {
+      const int cand = ctrl->cand_idx;
+      if (cand < n_items) {
+        async_commit_wait();
+        if ((int64_t)j_step < ctrl->cand_steps) {
+          ctrl->nx_idx = cand;
+          ctrl->nx_ti = ctrl->cand_ti;
+          ctrl->nx_tiles_x = ctrl->cand_tiles_x;
+          ctrl->nx_parity = ctrl->cand_parity;
+          ctrl->nx_tmap = ctrl->cand_tmap;
+        } else {
+          scan(cand + gridDim.x);
+        }
+      } else {
+        ctrl->nx_idx = n_items;
+      }
+    }
   }
 }
 

@@ -62,7 +62,9 @@ struct Inst1D {
   Params<double> pd;
 };
 
-struct Inst2D {
+// 16-byte aligned and sized, so a kernel can fetch a descriptor into shared memory with one bulk
+// copy.
+struct alignas(16) Inst2D {
   void* u[2];         // ping-pong complex state buffers, n x n, row-major (x contiguous)
   const void* P;      // pump, n x n
   int n;

@@ -159,7 +159,7 @@ static int choose_shape(int dtype, int n, int K, int variant) {
     if (!tile_supported(variant, dtype)) return -1;
     return variant;
   }
-  if (dtype == NLS_C64) return TILE_64xO64;
+  if (dtype == NLS_C64) return TILE_R64x96S;
   return (K == 1 && n >= 1024) ? TILE_32x32 : TILE_UNFUSED;
 }
 
