@@ -4,20 +4,25 @@ For each (dimension, precision, stencil order, grid-size bucket) it times the ca
 variants on a seeded instance of that size and keeps the fastest:
 
 * 2-D: 0 = unfused (four stage launches per step, no halo recomputation), or a fused
-  single-pass step with tile region 64x64 / 512 threads (1), 128x32 / 512 (2), 32x32 / 256 (3),
-  64x64 / 1024 (4) or 128x32 / 1024 (5);
+  single-pass step: column-strip tiles (rk4_2d_fused) with region 64x64 / 512 threads (1),
+  128x32 / 512 (2), 32x32 / 256 (3), 64x64 / 1024 (4), 128x32 / 1024 (5), 64x(64+8K) / 512 (6) or
+  768/640 (7), or register-resident row-strip tiles (rk4_2d_reg, complex64) with region 64x80 /
+  512 (8), 64x96 / 384 (9), 64x96 / 256 (10) or 64x64 / 512 (11);
 * 1-D: the resident kernel on 1, 2, 4, 8 or 16 CTAs of a cluster, or 0 = unfused stage kernels.
 
 Two objectives: ``mode="single"`` times one solve of the size (latency of a lone solve), and
 ``mode="batch"`` times a batch of copies large enough to fill the GPU (throughput per node-step,
 what a batched or served mix cares about: a shape with less halo recomputation wins there even
-when it exposes fewer tiles per grid).  Results are cached per GPU name in a JSON file
-(``NLS_GB300_TUNE_CACHE`` or ``~/.cache/nls_gb300/autotune.json``); ``apply(specs, dtype, mode)``
-fills ``Spec.variant``.  Timings use CUDA events on the library's stream.
+when it exposes fewer tiles per grid).  For a batch, ``apply`` also times the batch's own 2-D
+specs under one shared shape (one persistent launch per step instead of one per shape) against
+the per-size choices and keeps the faster.  Per-size results are cached per GPU name in a JSON
+file (``NLS_GB300_TUNE_CACHE`` or ``~/.cache/nls_gb300/autotune.json``); ``apply(specs, dtype,
+mode)`` fills ``Spec.variant``.  Timings use CUDA events on the library's stream.
 """
 
 from __future__ import annotations
 
+import copy
 import json
 import os
 import threading
@@ -142,12 +147,92 @@ def tune(dim: int, n: int, order: int, dtype=np.complex64, steps: int = 128, dev
     return int(best)
 
 
-def apply(specs, dtype=np.complex64, device: int = 0, mode: str = "batch"):
-    """Set each Spec.variant from the tuned choice for its size bucket; returns the choices."""
-    memo = {}
+def _time_mix(specs, dtype, variant, steps, device):
+    """ms per node-step of one batch of exactly these specs with the 2-D variant forced."""
+    trial = []
     for s in specs:
+        t = copy.copy(s)
+        t.variant = variant
+        trial.append(t)
+    return _time_mix_assigned(trial, dtype, steps, device)
+
+
+def tune_mix(specs, dtype=np.complex64, steps: int = 32, device: int = 0):
+    """One 2-D tile shape for a whole batch of 2-D specs of one stencil order, timed on that batch.
+
+    All of the batch's 2-D tiles then go to a single persistent launch per step, which balances
+    better over the SMs than one launch per shape."""
+    times = {}
+    n_max = max(s.n for s in specs)
+    for v in candidates(2, dtype, bucket(n_max)):
+        if v == 0:
+            continue
+        try:
+            times[v] = _time_mix(specs, dtype, v, steps, device)
+        except ValueError:
+            continue
+    best = min(times, key=times.get)
+    return int(best), times
+
+
+def apply(specs, dtype=np.complex64, device: int = 0, mode: str = "batch"):
+    """Set each Spec.variant from the tuned choice; returns the choices.
+
+    1-D specs: the fastest cluster size of their size bucket.  2-D specs: per size bucket in
+    ``single`` mode; in ``batch`` mode one shape per stencil order, timed on the batch itself
+    (``tune_mix``), unless the per-bucket choices together time faster on it."""
+    memo = {}
+    out = {}
+    two_d = {}
+    for s in specs:
+        if s.dim == 2 and mode == "batch":
+            two_d.setdefault(s.order, []).append(s)
+            continue
         k = (s.dim, s.order, bucket(s.n))
         if k not in memo:
             memo[k] = tune(s.dim, s.n, s.order, dtype=dtype, device=device, mode=mode)
         s.variant = memo[k]
-    return {f"{d}d/o{o}/n<={b}": v for (d, o, b), v in sorted(memo.items())}
+    for (d, o, b), v in sorted(memo.items()):
+        out[f"{d}d/o{o}/n<={b}"] = v
+    for order, group in sorted(two_d.items()):
+        best, times = tune_mix(group, dtype=dtype, device=device)
+        # per-bucket choices as one more candidate
+        per = {}
+        for s in group:
+            k = (order, bucket(s.n))
+            if k not in per:
+                per[k] = tune(2, s.n, order, dtype=dtype, device=device, mode="batch")
+        trial = [copy.copy(s) for s in group]
+        for t in trial:
+            t.variant = per[(order, bucket(t.n))]
+        t_per = _time_mix_assigned(trial, dtype, 32, device)
+        if t_per < times[best]:
+            for s in group:
+                s.variant = per[(order, bucket(s.n))]
+            for (o, b), v in sorted(per.items()):
+                out[f"2d/o{o}/n<={b}"] = v
+        else:
+            for s in group:
+                s.variant = best
+            out[f"2d/o{order}/mix"] = best
+    return out
+
+
+def _time_mix_assigned(specs, dtype, steps, device):
+    """ms per node-step of one batch of these specs with their own variants."""
+    import torch
+
+    from . import device as ndev
+    from .batch import BatchSolver
+    b = BatchSolver(specs, dtype=dtype, device=device)
+    try:
+        b.run(steps)
+        ext = ndev.stream(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        b.run(steps)
+        e1.record(ext)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / (steps * sum(s.nodes for s in specs))
+    finally:
+        b.close()

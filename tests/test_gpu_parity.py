@@ -334,3 +334,21 @@ def test_precision_form_with_fp64_diagnostics(gpu, oracle_lib):
     want = oracle_lib.chemical_potential(s.dx, s.pumping, s.coeffs, u, dtype=np.float64)
     assert abs(res["log"][-1]["mu"] - want) <= 1e-5 * abs(want)
     np.testing.assert_allclose(res["log"][-1]["norm"], np.sum(np.abs(u) ** 2) * s.dx ** 2, rtol=1e-12)
+
+
+def test_autotune_batch_mode_assigns_valid_variants(gpu, tmp_path, monkeypatch):
+    """Batch-mode tuning gives every spec a candidate variant, and the tuned batch matches single solves."""
+    from nls_gb300 import autotune
+    from nls_gb300 import workloads as w
+    from nls_gb300.batch import BatchSolver
+    monkeypatch.setenv("NLS_GB300_TUNE_CACHE", str(tmp_path / "tune.json"))
+    specs = [w.mix_instance(i, 1) for i in range(3)] + [w.mix_instance(10 + i, 2) for i in range(4)]
+    got = autotune.apply(specs, dtype=np.complex64, mode="batch")
+    assert got
+    for s in specs:
+        assert s.variant in autotune.candidates(s.dim, np.complex64, autotune.bucket(s.n))
+    b = BatchSolver(specs, dtype=np.complex64)
+    b.run(30)
+    for i, s in enumerate(specs):
+        want = _device_solve(gpu, s, 30, np.complex64, s.variant)
+        assert np.array_equal(b.get(i), want.astype(np.complex64)), i
