@@ -178,10 +178,15 @@ def oracle_sample(specs):
     return [s for i, s in enumerate(specs) if i % 4 == 0]
 
 
-def calibrated_steps(specs, threads, target_s=20.0):
+def calibrated_steps(specs, threads, target_s=20.0, max_steps=2000):
     """RK4 steps per CPU sample so that one sample takes about target_s seconds."""
-    _, t1 = cpu_oracle_rate(specs, 1, threads)
-    return int(min(2000, max(1, round(target_s / max(t1, 1e-3)))))
+    steps = 1
+    while True:   # grow the probe until it runs long enough to time
+        _, t = cpu_oracle_rate(specs, steps, threads)
+        if t > 0.25 or steps >= max_steps:
+            break
+        steps *= 4
+    return int(min(max_steps, max(1, round(steps * target_s / max(t, 1e-6)))))
 
 
 def run_reference(args):
@@ -214,6 +219,31 @@ def run_reference(args):
                 "restatement of nls/nls.f90 is timed instead",
     }
     print(json.dumps(line))
+    return 0
+
+
+def run_cpu(args):
+    """--workload cpu: the reference algorithm (the float32 oracle, a C++ restatement of
+    nls/nls.f90) on this host's cores for configs 0-2, on 1 thread (the reference is
+    single-threaded) and on all cores (OpenMP over 2-D columns; a 1-D solve stays sequential),
+    each a bounded sample of about 3 s of RK4 steps; one JSON line."""
+    from nls_gb300 import workloads
+    cores = os.cpu_count() or 1
+    cases = [("config 0: 1-D 1000 nodes on [0,40], order 5, complex64", workloads.plain_1d()[0]),
+             ("config 1: 2-D 256^2 on [-20,20]^2, order 3, complex64", workloads.plain_2d()[0]),
+             ("config 2: 2-D 1024^2 on [-40,40]^2, order 5, complex64", workloads.precision_2d()[0])]
+    out = []
+    for name, spec in cases:
+        for threads in sorted({1, cores}):
+            if spec.dim == 1 and threads > 1:
+                continue
+            steps = calibrated_steps([spec], threads, target_s=3.0, max_steps=100000)
+            rate, secs = cpu_oracle_rate([spec], steps, threads)
+            out.append({"case": name, "threads": threads, "steps": steps, "seconds": secs,
+                        "node_steps_per_s": rate})
+    print(json.dumps({"workload": "cpu", "kind": "port", "cores": cores,
+                      "note": "float32 oracle (the reference's algorithm and precision); the "
+                              "reference's Fortran cannot be compiled here", "results": out}))
     return 0
 
 
@@ -515,7 +545,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
     ap.add_argument("--quick", action="store_true",
                     help="timed batched solves only (no roofline, accuracy, e2e, serve or CPU legs)")
-    ap.add_argument("--workload", choices=["batch", "grid1d", "grid2d", "precision2d", "serve"], default="batch")
+    ap.add_argument("--workload", choices=["batch", "grid1d", "grid2d", "precision2d", "serve", "cpu"],
+                    default="batch")
     ap.add_argument("--chunk", type=int, default=500, help="serving pool chunk (RK4 steps per scheduling round)")
     ap.add_argument("--solve-steps", type=int, default=SOLVE_STEPS, help="RK4 steps per solve")
     ap.add_argument("--n", type=int, default=4096, help="grid size for grid1d/grid2d")
@@ -532,6 +563,8 @@ def main():
         return run_precision(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "cpu":
+        return run_cpu(args)
     if args.workload != "batch":
         return run_grid(args)
     return run_ours(args)

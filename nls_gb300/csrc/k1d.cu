@@ -116,6 +116,11 @@ __global__ void __launch_bounds__(512) rk4_1d_resident(const Inst1D* __restrict_
 
   C u[NPT], acc[NPT];
   T P[NPT], ir[NPT];
+  // Double precision: each node's full operator row (w2 + w1 / (p h), as in the band matrix, or
+  // the near-axis row), built once per launch, so a stage evaluates one (2K+1)-term dot product
+  // per node instead of separate D2 and D1 sums (FP64 runs at a small fraction of FP32 on GB300).
+  constexpr bool ROWS = sizeof(T) == 8;
+  T wrow[ROWS ? NPT : 1][2 * K + 1];
 #pragma unroll
   for (int j = 0; j < NPT; ++j) {
     const int li = tid + j * NT;
@@ -123,11 +128,20 @@ __global__ void __launch_bounds__(512) rk4_1d_resident(const Inst1D* __restrict_
     acc[j] = mk<T>(0, 0);
     P[j] = 0;
     ir[j] = 0;
+    if (ROWS) {
+#pragma unroll
+      for (int i = 0; i < 2 * K + 1; ++i) wrow[ROWS ? j : 0][i] = 0;
+    }
     if (li < len) {
       const int p = p0 + li;
       u[j] = Ug[p];
       P[j] = Pg[p];
       ir[j] = p >= K ? (T)1 / ((T)p * h) : (T)0;
+      if (ROWS) {
+#pragma unroll
+        for (int i = 0; i < 2 * K + 1; ++i)
+          wrow[ROWS ? j : 0][i] = p >= K ? w.w1[i] / ((T)p * h) + w.w2[i] : ParamsOf<T>::near(I.op, p, i);
+      }
       buf[0][K + li] = u[j];
       if (left_buf[0] && li < K) left_buf[0][seg + K + li] = u[j];
       if (right_buf[0] && li >= seg - K) right_buf[0][li - (seg - K)] = u[j];
@@ -166,7 +180,16 @@ __global__ void __launch_bounds__(512) rk4_1d_resident(const Inst1D* __restrict_
 #pragma unroll
         for (int i = 0; i < CB; ++i) {
           const int p = p0 + tid + (j0 + i) * NT;
-          if (p >= K) {
+          if (ROWS) {
+            T lx = 0, ly = 0;
+#pragma unroll
+            for (int d = 0; d < 2 * K + 1; ++d) {
+              lx += wrow[ROWS ? j0 + i : 0][d] * v[i][d].x;
+              ly += wrow[ROWS ? j0 + i : 0][d] * v[i][d].y;
+            }
+            lu[i].x = lx;
+            lu[i].y = ly;
+          } else if (p >= K) {
             T d2x = 0, d2y = 0, d1x = 0, d1y = 0;
 #pragma unroll
             for (int d = -K; d <= K; ++d) {
@@ -290,6 +313,9 @@ __global__ void __launch_bounds__(512) rk4_1d_cluster_tb(const Inst1D* __restric
   // owned local indices li = tid + j*NT - H, j < NPT, covering [-H, seg + H)
   C u[NPT], acc[NPT];
   T pc[NPT], ir[NPT];
+  // double precision: each node's full operator row, built once per launch (see rk4_1d_resident)
+  constexpr bool ROWS = sizeof(T) == 8;
+  T wrow[ROWS ? NPT : 1][2 * K + 1];
   unsigned indom = 0;
 #pragma unroll
   for (int j = 0; j < NPT; ++j) {
@@ -300,14 +326,29 @@ __global__ void __launch_bounds__(512) rk4_1d_cluster_tb(const Inst1D* __restric
     u[j] = in ? Ug[p] : mk<T>(0, 0);
     pc[j] = in ? ph.c12 * Pg[p] : (T)0;
     ir[j] = (in && p >= K) ? (T)1 / ((T)p * h) : (T)0;
+    if (ROWS) {
+#pragma unroll
+      for (int i = 0; i < 2 * K + 1; ++i)
+        wrow[ROWS ? j : 0][i] = !in ? (T)0 : (p >= K ? w.w1[i] / ((T)p * h) + w.w2[i] : ParamsOf<T>::near(I.op, p, i));
+    }
     acc[j] = mk<T>(0, 0);
     if (in) A[0][li] = u[j];
   }
   __syncthreads();
 
-  auto lap = [&](const C* in, int li, int p, T irv) -> C {
+  auto lap = [&](const C* in, int li, int p, T irv, int j) -> C {
     C lu;
-    if (p >= K) {
+    if (ROWS) {
+      T lx = 0, ly = 0;
+#pragma unroll
+      for (int d = -K; d <= K; ++d) {
+        const C v = in[li + d];
+        lx += wrow[ROWS ? j : 0][d + K] * v.x;
+        ly += wrow[ROWS ? j : 0][d + K] * v.y;
+      }
+      lu.x = lx;
+      lu.y = ly;
+    } else if (p >= K) {
       T d2x = 0, d2y = 0, d1x = 0, d1y = 0;
 #pragma unroll
       for (int d = -K; d <= K; ++d) {
@@ -369,7 +410,7 @@ __global__ void __launch_bounds__(512) rk4_1d_cluster_tb(const Inst1D* __restric
         const int li = tid + j * NT - H;
         if (((indom >> j) & 1u) && li >= lo && li < hi) {
           const int p = p0 + li;
-          const C k = kval(in[li], pc[j], lap(in, li, p, ir[j]));
+          const C k = kval(in[li], pc[j], lap(in, li, p, ir[j], j));
           if (s == 1) acc[j] = k;
           else {
             acc[j].x += wk * k.x;
