@@ -249,6 +249,30 @@ def run_cpu(args):
 
 # ------------------------------------------------------------------ GPU legs
 
+def pinned_fields(specs, ctype, rtype):
+    """Per-instance pump, initial-state and output arrays in one pinned (page-locked) host block,
+    laid out as the C ABI reads them (Fortran order in 2-D), inputs filled from the specs."""
+    import torch
+    sizes = []
+    for s in specs:
+        sizes += [s.nodes * np.dtype(rtype).itemsize, s.nodes * np.dtype(ctype).itemsize,
+                  s.nodes * np.dtype(ctype).itemsize]
+    offs = np.concatenate([[0], np.cumsum([(b + 255) // 256 * 256 for b in sizes])])
+    block = torch.empty(int(offs[-1]), dtype=torch.uint8, pin_memory=True).numpy()
+    views = []
+    for k, s in enumerate(specs):
+        shape = (s.n, s.n) if s.dim == 2 else (s.n,)
+        order = "F" if s.dim == 2 else "C"
+        for j, dt in enumerate((rtype, ctype, ctype)):
+            o = int(offs[3 * k + j])
+            views.append(np.ndarray(shape, dtype=dt, buffer=block, offset=o, order=order))
+    P, U, O = views[0::3], views[1::3], views[2::3]
+    for s, p, u in zip(specs, P, U):
+        p[...] = np.asarray(s.pumping)
+        u[...] = np.asarray(s.u0)
+    return P, U, O
+
+
 def run_grid(args):
     """--workload grid1d|grid2d: one solve of one grid (profiling and single-solve roofline)."""
     import torch
@@ -492,22 +516,25 @@ def run_ours(args):
     result["rel_l2_vs_c128"] = {"density_max": max(errs_d), "reservoir_max": max(errs_n),
                                 "sample": f"same {len(sample_idx)} instances after {SOLVE_STEPS} steps"}
 
-    # ---- end to end through the host-buffer C ABI: upload u0 and P, solve, download every state
+    # ---- end to end through the host-buffer C ABI: upload u0 and P from pinned host memory,
+    # solve, download every state into pinned host memory
     h2d = sum(s.nodes * (8 + 4) for s in specs)
     d2h = sum(s.nodes * 8 for s in specs)
+    hP, hU, hO = pinned_fields(specs, np.complex64, np.float32)
     e2e_times = []
     for rep in range(max(1, min(args.steps, 2))):
         ctx = b.ctx
         ctx.synchronize()
         t0 = time.perf_counter()
-        for i, s in enumerate(specs):
-            b.set(i, s.pumping, s.u0)
+        for i in range(len(specs)):
+            b.set(i, hP[i], hU[i])
         b.run(SOLVE_STEPS)
-        outs = [b.get(i) for i in range(len(specs))]
+        for i in range(len(specs)):
+            b.get(i, out=hO[i])
         e2e_times.append(time.perf_counter() - t0)
     e2e = float(total_nodes) * SOLVE_STEPS / float(np.mean(e2e_times))
     result["e2e"] = {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                     "path": "nls_batch_set (host u0, P) -> nls_batch_run(5000) -> nls_batch_get (host u)"}
+                     "path": "nls_batch_set (pinned host u0, P) -> nls_batch_run(5000) -> nls_batch_get (pinned host u)"}
     del outs
 
     # ---- served stream (continuous batching) p50/p99

@@ -71,9 +71,17 @@ class BatchSolver:
     def synchronize(self):
         self.ctx.synchronize()
 
-    def get(self, i: int) -> np.ndarray:
+    def get(self, i: int, out: np.ndarray = None) -> np.ndarray:
+        """State of instance i; into ``out`` if given (the instance's shape and complex dtype,
+        Fortran order in 2-D, e.g. a view of pinned host memory), else into a new array."""
         s = self.specs[i]
-        out = np.empty((s.n, s.n) if s.dim == 2 else (s.n,), dtype=self.ctype, order="F" if s.dim == 2 else "C")
+        shape = (s.n, s.n) if s.dim == 2 else (s.n,)
+        if out is None:
+            out = np.empty(shape, dtype=self.ctype, order="F" if s.dim == 2 else "C")
+        elif (out.shape != shape or out.dtype != self.ctype or
+              not (out.flags.f_contiguous if s.dim == 2 else out.flags.c_contiguous)):
+            raise ValueError(f"instance {i}: out must be {shape} {np.dtype(self.ctype).name}, "
+                             f"{'Fortran' if s.dim == 2 else 'C'} order")
         _lib.check(_lib.lib().nls_batch_get(self.handle, i, _lib.ptr(out)), "nls_batch_get", self.ctx.handle)
         return out
 
