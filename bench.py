@@ -535,7 +535,7 @@ def run_ours(args):
     e2e = float(total_nodes) * SOLVE_STEPS / float(np.mean(e2e_times))
     result["e2e"] = {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                      "path": "nls_batch_set (pinned host u0, P) -> nls_batch_run(5000) -> nls_batch_get (pinned host u)"}
-    del outs
+    del hP, hU, hO
 
     # ---- served stream (continuous batching) p50/p99
     if args.serve > 0:
