@@ -175,7 +175,7 @@ __device__ __forceinline__ void reg_stage(float2 (&tX)[NJ], float2 (&tY)[NJ], fl
     const float2 den = fma2(c.c14, sq, c.c13);
     const float2 r = mul2(pc[j], f2(rcp_approx(den.x), rcp_approx(den.y)));
     const float2 a = fma2(c.c3, r, c.nc4);
-    const float2 bw = add2(fma2(c.c5, sq, mul2(c.c6, r)), c.nwc);
+    const float2 bw = fma2(c.c5, sq, fma2(c.c6, r, c.nwc));
     const float2 kX = fma2(a, X, fma2(bw, Y, neg2(mY)));
     const float2 kY = fma2(a, Y, fma2(neg2(bw), X, mX));
     if (S == 1) {

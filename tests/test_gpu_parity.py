@@ -352,3 +352,18 @@ def test_autotune_batch_mode_assigns_valid_variants(gpu, tmp_path, monkeypatch):
     for i, s in enumerate(specs):
         want = _device_solve(gpu, s, 30, np.complex64, s.variant)
         assert np.array_equal(b.get(i), want.astype(np.complex64)), i
+
+
+@pytest.mark.parametrize("variant", [8, 10])
+@pytest.mark.parametrize("order", [3, 5])
+@pytest.mark.parametrize("n", [5, 33, 64, 97, 200])
+def test_2d_c64_register_tiles_small_and_ragged(gpu, oracle_lib, variant, order, n):
+    """Register-resident tiles on grids smaller than one region, odd sides (plain loads) and
+    multiples of 4 (TMA), against the FP32 oracle."""
+    if n < order:
+        pytest.skip("grid smaller than the stencil")
+    s = _spec_2d(n, order)
+    iters = 60
+    want32 = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float32)
+    got = _device_solve(gpu, s, iters, np.complex64, variant)
+    assert rel(got, want32) <= 3e-5
