@@ -152,8 +152,8 @@ __device__ __forceinline__ void reg_stage(float2 (&tX)[NJ], float2 (&tY)[NJ], fl
       // left neighbour of the pair's first node, right neighbour of its second
       const float lx = __shfl_up_sync(0xffffffffu, X.y, 1), ly = __shfl_up_sync(0xffffffffu, Y.y, 1);
       const float rx = __shfl_down_sync(0xffffffffu, X.x, 1), ry = __shfl_down_sync(0xffffffffu, Y.x, 1);
-      const float2 sX = add2(f2(lx + X.y, X.x + rx), add2(rowX(j - 1), rowX(j + 1)));
-      const float2 sY = add2(f2(ly + Y.y, Y.x + ry), add2(rowY(j - 1), rowY(j + 1)));
+      const float2 sX = add2(add2(f2(lx + X.y, X.x + rx), rowX(j - 1)), rowX(j + 1));
+      const float2 sY = add2(add2(f2(ly + Y.y, Y.x + ry), rowY(j - 1)), rowY(j + 1));
       mX = mul2(c.w1, sX);
       mY = mul2(c.w1, sY);
     } else {
