@@ -162,10 +162,10 @@ __device__ __forceinline__ void reg_stage(float2 (&tX)[NJ], float2 (&tY)[NJ], fl
       const float2 LY = f2(__shfl_up_sync(0xffffffffu, Y.x, 1), __shfl_up_sync(0xffffffffu, Y.y, 1));
       const float2 RX = f2(__shfl_down_sync(0xffffffffu, X.x, 1), __shfl_down_sync(0xffffffffu, X.y, 1));
       const float2 RY = f2(__shfl_down_sync(0xffffffffu, Y.x, 1), __shfl_down_sync(0xffffffffu, Y.y, 1));
-      const float2 s1X = add2(f2(LX.y + X.y, X.x + RX.x), add2(rowX(j - 1), rowX(j + 1)));
-      const float2 s1Y = add2(f2(LY.y + Y.y, Y.x + RY.x), add2(rowY(j - 1), rowY(j + 1)));
-      const float2 s2X = add2(add2(LX, RX), add2(rowX(j - 2), rowX(j + 2)));
-      const float2 s2Y = add2(add2(LY, RY), add2(rowY(j - 2), rowY(j + 2)));
+      const float2 s1X = add2(add2(f2(LX.y + X.y, X.x + RX.x), rowX(j - 1)), rowX(j + 1));
+      const float2 s1Y = add2(add2(f2(LY.y + Y.y, Y.x + RY.x), rowY(j - 1)), rowY(j + 1));
+      const float2 s2X = add2(add2(add2(LX, RX), rowX(j - 2)), rowX(j + 2));
+      const float2 s2Y = add2(add2(add2(LY, RY), rowY(j - 2)), rowY(j + 2));
       mX = fma2(c.w2, s2X, mul2(c.w1, s1X));
       mY = fma2(c.w2, s2Y, mul2(c.w1, s1Y));
     }
