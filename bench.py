@@ -52,7 +52,8 @@ SHAPE_KERNELS = {
     5: "rk4_2d_fused 128x32, 1024 threads", 6: "rk4_2d_fused 64x(64+8K), 512 threads",
     7: "rk4_2d_fused 64x(64+8K), 768/640 threads", 8: "rk4_2d_reg 64x80, 16 warps x 5 rows",
     9: "rk4_2d_reg 64x96, 12 warps x 8 rows", 10: "rk4_2d_reg 64x96, 8 warps x 12 rows",
-    11: "rk4_2d_reg 64x64, 16 warps x 4 rows",
+    11: "rk4_2d_reg 64x64, 16 warps x 4 rows", 12: "rk4_2d_reg 64x72, 8 warps x 9 rows",
+    13: "rk4_2d_reg 64x72, 12 warps x 6 rows", 14: "rk4_2d_reg 64x80, 8 warps x 10 rows",
 }
 DEFAULT_SHAPE_C64 = 10
 

@@ -50,7 +50,8 @@ typedef struct nls_pool nls_pool;
  * 2 = 128x32 (512), 3 = 32x32 (256), 4 = 64x64 (1024), 5 = 128x32 (1024),
  * 6 = 64 x (64 + 8K) with output tiles exactly 64 rows high (512), 7 = the same region with 768
  * (order 3) or 640 (order 5) threads; register-resident tiles (complex64 only), region 64 wide:
- * 8 = 64x80 (512), 9 = 64x96 (384), 10 = 64x96 (256), 11 = 64x64 (512). */
+ * 8 = 64x80 (512), 9 = 64x96 (384), 10 = 64x96 (256), 11 = 64x64 (512), 12 = 64x72 (256),
+ * 13 = 64x72 (384), 14 = 64x80 (256). */
 typedef struct nls_problem {
   int dim;
   int n;

@@ -421,13 +421,15 @@ __global__ void __launch_bounds__(256) rhs_2d(int n, const void* __restrict__ u_
 //   TILE_128x32W : 128 x 32, 8 strips of 4 rows  (1024 threads)
 //   TILE_64xO64  : 64 x (64 + 8K), 8 strips (512 threads): output tiles exactly 64 rows high
 //   TILE_64xO64M : the same region with 12 (K = 1) or 10 (K = 2) strips (768 / 640 threads)
-//   TILE_R64x*   : rk4_2d_reg, region 64 x (warps x rows per warp), see k2d_reg.cuh
+//   TILE_R64x*   : rk4_2d_reg, region 64 x (warps x rows per warp), see k2d_reg.cuh; 72 and 80
+//                  rows give output tiles exactly 64 rows high at order 3 and 5
 int tile_region_x(int shape) {
   switch (shape) {
     case TILE_64x64: return 64; case TILE_128x32: return 128; case TILE_32x32: return 32;
     case TILE_64x64W: return 64; case TILE_128x32W: return 128;
     case TILE_64xO64: return 64; case TILE_64xO64M: return 64;
-    case TILE_R64x80: case TILE_R64x96: case TILE_R64x96S: case TILE_R64x64: return 64;
+    case TILE_R64x80: case TILE_R64x96: case TILE_R64x96S: case TILE_R64x64: case TILE_R64x72:
+    case TILE_R64x72W: case TILE_R64x80S: return 64;
   }
   return 0;
 }
@@ -438,11 +440,12 @@ int tile_region_y(int shape, int K) {
     case TILE_64xO64: return 64 + 8 * K; case TILE_64xO64M: return 64 + 8 * K;
     case TILE_R64x80: return 80; case TILE_R64x96: return 96; case TILE_R64x96S: return 96;
     case TILE_R64x64: return 64;
+    case TILE_R64x72: case TILE_R64x72W: return 72; case TILE_R64x80S: return 80;
   }
   return 0;
 }
 static bool reg_shape(int shape) {
-  return shape == TILE_R64x80 || shape == TILE_R64x96 || shape == TILE_R64x96S || shape == TILE_R64x64;
+  return shape >= TILE_R64x80 && shape <= TILE_R64x80S;
 }
 int tile_out_x(int shape, int K) { return tile_region_x(shape) - 8 * K; }
 int tile_out_y(int shape, int K) { return tile_region_y(shape, K) - 8 * K; }
@@ -517,6 +520,9 @@ static int occ_r() {
     case TILE_R64x96: return CALL<K, 12, 8, TMA>(__VA_ARGS__);             \
     case TILE_R64x96S: return CALL<K, 8, 12, TMA>(__VA_ARGS__);            \
     case TILE_R64x64: return CALL<K, 16, 4, TMA>(__VA_ARGS__);             \
+    case TILE_R64x72: return CALL<K, 8, 9, TMA>(__VA_ARGS__);              \
+    case TILE_R64x72W: return CALL<K, 12, 6, TMA>(__VA_ARGS__);            \
+    case TILE_R64x80S: return CALL<K, 8, 10, TMA>(__VA_ARGS__);            \
   }
 
 #define NLSG_SHAPES(T, K, CALL, ...)                                        \

@@ -41,6 +41,9 @@ enum TileShape2D {
   TILE_R64x96 = 9,    // 12 warps x 8 rows (384 threads)
   TILE_R64x96S = 10,  // 8 warps x 12 rows (256 threads)
   TILE_R64x64 = 11,   // 16 warps x 4 rows (512 threads)
+  TILE_R64x72 = 12,   // 8 warps x 9 rows (256 threads): 64 output rows at order 3
+  TILE_R64x72W = 13,  // 12 warps x 6 rows (384 threads)
+  TILE_R64x80S = 14,  // 8 warps x 10 rows (256 threads): 64 output rows at order 5
 };
 int tile_region_x(int shape);
 int tile_region_y(int shape, int K);

@@ -164,7 +164,7 @@ def _oracle_2d_pair(oracle_lib, s, order, iters):
 # n = 150: plain global loads (rows not 16-byte multiples); n = 152: the TMA tile path
 @pytest.mark.parametrize("n", [150, 152])
 @pytest.mark.parametrize("order", [3, 5])
-@pytest.mark.parametrize("variant", [-1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11])
+@pytest.mark.parametrize("variant", [-1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14])
 def test_2d_c64_vs_oracles(gpu, oracle_lib, order, variant, n):
     s = _spec_2d(n, order)
     iters = 400
@@ -354,7 +354,7 @@ def test_autotune_batch_mode_assigns_valid_variants(gpu, tmp_path, monkeypatch):
         assert np.array_equal(b.get(i), want.astype(np.complex64)), i
 
 
-@pytest.mark.parametrize("variant", [8, 10])
+@pytest.mark.parametrize("variant", [8, 10, 12])
 @pytest.mark.parametrize("order", [3, 5])
 @pytest.mark.parametrize("n", [5, 33, 64, 97, 200])
 def test_2d_c64_register_tiles_small_and_ragged(gpu, oracle_lib, variant, order, n):
