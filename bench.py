@@ -355,6 +355,13 @@ def run_serve(args):
     from nls_gb300.serve import Pool, serve
     count = args.serve if args.serve > 0 else 10000
     reqs = workloads.serve_stream(count)
+    tuned = None
+    if args.autotune:
+        # kernel variants tuned on the batched mix, which has the stream's size and parameter
+        # distribution
+        from nls_gb300 import autotune
+        tuned = autotune.apply(workloads.batch_mix(), dtype=np.complex64, device=local, mode="batch")
+        autotune.assign([spec for spec, _ in reqs], tuned)
     pool = Pool(dtype=np.complex64, budget_bytes=80 << 30, chunk_steps=args.chunk, device=local)
     st = serve(reqs, rate=200.0, pool=pool)
     pool.close()
@@ -377,7 +384,8 @@ def run_serve(args):
                       "max_ms": float(np.max(lat) * 1e3), "wall_s": st["wall_s"],
                       "node_steps_per_s": st["node_steps_per_s"], "node_steps": st["node_steps"],
                       "plain_c128_sequential_node_steps_per_s": plain_ns / plain_s,
-                      "plain_c128_sample": "24 requests of the stream solved one after another"}))
+                      "plain_c128_sample": "24 requests of the stream solved one after another",
+                      "autotuned_variants": tuned}))
     return 0
 
 
@@ -542,6 +550,9 @@ def run_ours(args):
     if args.serve > 0:
         from nls_gb300.serve import Pool, serve
         reqs = workloads.serve_stream(args.serve)
+        if tuned:
+            from nls_gb300 import autotune
+            autotune.assign([spec for spec, _ in reqs], tuned)
         pool = Pool(dtype=np.complex64, budget_bytes=80 << 30, chunk_steps=500, device=local)
         st = serve(reqs, rate=200.0, pool=pool)
         pool.close()

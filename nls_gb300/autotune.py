@@ -237,3 +237,17 @@ def _time_mix_assigned(specs, dtype, steps, device):
         return e0.elapsed_time(e1) / (steps * sum(s.nodes for s in specs))
     finally:
         b.close()
+
+
+def assign(specs, choices):
+    """Apply the choices ``apply`` returned (for one population) to other specs of the same
+    population, e.g. the requests of a served stream: per size bucket, or the shared 2-D shape of
+    a stencil order ("2d/o3/mix").  Specs with no matching choice keep their variant."""
+    for s in specs:
+        key = f"{s.dim}d/o{s.order}/n<={bucket(s.n)}"
+        mix = f"{s.dim}d/o{s.order}/mix"
+        if key in choices:
+            s.variant = int(choices[key])
+        elif mix in choices:
+            s.variant = int(choices[mix])
+    return specs

@@ -175,3 +175,15 @@ def test_solution_reservoir_density_and_mat_roundtrip(tmp_path):
     s2 = Solution(m2).restore(f2)
     np.testing.assert_allclose(s2.getSolution(), psi)
     assert s2.getElapsedTime() == 1.5
+
+
+def test_autotune_assign_maps_choices_to_other_specs():
+    """Choices tuned on one population are applied by size bucket, or by the shared 2-D shape."""
+    from nls_gb300 import autotune
+    from nls_gb300 import workloads as w
+    specs = [w.mix_instance(i, 1, with_data=False) for i in range(4)] + \
+            [w.mix_instance(10 + i, 2, with_data=False) for i in range(4)]
+    choices = {f"1d/o5/n<={autotune.bucket(s.n)}": 4 for s in specs if s.dim == 1}
+    choices["2d/o3/mix"] = 12
+    autotune.assign(specs, choices)
+    assert all(s.variant == (4 if s.dim == 1 else 12) for s in specs)
