@@ -160,7 +160,9 @@ static int choose_shape(int dtype, int n, int K, int variant) {
     return variant;
   }
   if (dtype == NLS_C64) return TILE_R64x96S;
-  return (K == 1 && n >= 1024) ? TILE_32x32 : TILE_UNFUSED;
+  // complex128 is FP64-bound on GB300: the stage kernels (no halo recomputation) beat the fused
+  // tile at every size measured (256^2 .. 1024^2, orders 3 and 5)
+  return TILE_UNFUSED;
 }
 
 // ------------------------------------------------------------------ graph helpers
