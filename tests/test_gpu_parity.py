@@ -270,10 +270,15 @@ def _mixed_specs(dtype):
     return specs
 
 
-@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
-def test_batch_matches_single_solves(gpu, dtype):
+@pytest.mark.parametrize("dtype,shape2d", [(np.complex64, -1), (np.complex64, 12), (np.complex64, 9),
+                                            (np.complex128, -1)])
+def test_batch_matches_single_solves(gpu, dtype, shape2d):
     from nls_gb300.batch import BatchSolver
     specs = _mixed_specs(dtype)
+    if shape2d > 0:
+        for s in specs[:-1]:          # the last one keeps its own 32x32 tile: two 2-D groups
+            if s.dim == 2:
+                s.variant = shape2d
     b = BatchSolver(specs, dtype=dtype)
     b.run(57)
     b.run(20)
