@@ -13,8 +13,11 @@
 //     registers; only the K rows at either end of a strip pass through shared memory, once per
 //     stage, for the strips above and below.
 // Shared memory then carries a few bytes per node-stage instead of every stencil operand, which
-// was the limiter of the column-strip layout.  The state and pump boxes of the next tile are
-// prefetched by TMA (cp.async.bulk.tensor) while the current one is computed.
+// was the limiter of the column-strip layout.  With TMA (grids whose rows are 16-byte multiples),
+// one elected thread fetches the next tile's state and pump boxes (cp.async.bulk.tensor) and its
+// instance descriptor (cp.async.bulk) on one mbarrier while the current tile is computed, and
+// looks up the work item after that with cp.async, so no thread waits on global memory at a tile
+// boundary; otherwise every thread loads its own node pairs from global memory.
 #pragma once
 
 namespace nlsg {
