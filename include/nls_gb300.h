@@ -187,6 +187,16 @@ int nls_pool_destroy(nls_pool* pool);
 int nls_solve_2d_noalloc(int dtype, const nls_problem* problem, int64_t iters,
                          const void* pumping_dev, void* u_dev, void* stream);
 
+/* ---- testing ----------------------------------------------------------------------------- */
+
+/* No counterpart in the reference.  Test control of the failure path of the bounded tile waits:
+ * with extra_bytes > 0 every complex64 register-tile launch on `device` (variants 8-14 on grids
+ * taking the TMA path) arms its tile barrier for extra_bytes more than its copies deliver, so the
+ * barrier never completes, each CTA gives up after its bounded wait (about a second), and the
+ * solve returns NLS_ERR_TIMEOUT; 0 restores normal operation.  No fault is raised and the
+ * context stays usable.  Not for production use. */
+int nls_test_set_tile_tx_extra(int device, unsigned extra_bytes);
+
 #ifdef __cplusplus
 }
 #endif

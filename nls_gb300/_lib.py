@@ -89,6 +89,7 @@ SIGNATURES = {
     "nls_pool_status": (_i, [_p, _pi, _psz]),
     "nls_pool_destroy": (_i, [_p]),
     "nls_solve_2d_noalloc": (_i, [_i, _pp, _i64, _p, _p, _p]),
+    "nls_test_set_tile_tx_extra": (_i, [_i, ctypes.c_uint]),
 }
 
 _lib = None

@@ -152,6 +152,9 @@ __device__ __forceinline__ void tile_stage(const typename C2<T>::type* __restric
 
 // Set when a bounded wait on a tile copy gives up; read and cleared by the host.
 __device__ int g_tile_wait_timeout = 0;
+// Extra bytes the register-tile kernel arms its tile barrier for (0 in normal operation): a test
+// control that makes the bounded wait expire without any fault.
+__device__ unsigned g_tile_tx_extra = 0;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -645,6 +648,10 @@ int tma_encode_2d(int shape, int K, int n, const void* u0, const void* u1, const
 }
 
 size_t tma_map_bytes() { return 3 * sizeof(CUtensorMap); }
+
+cudaError_t tile_tx_extra_set(unsigned bytes) {
+  return cudaMemcpyToSymbol(g_tile_tx_extra, &bytes, sizeof(bytes));
+}
 
 int tile_wait_timeout_read_clear(cudaStream_t s) {
   int v = 0, zero = 0;

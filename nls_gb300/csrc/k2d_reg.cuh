@@ -332,6 +332,7 @@ rk4_2d_reg(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items,
   // ---- TMA path: the elected thread (thread 0) keeps one tile in flight and looks up the one
   // after it while the current tile is computed.
   uint64_t* bar = &ctrl->bar;
+  const uint32_t tx_extra = threadIdx.x == 0 ? g_tile_tx_extra : 0u;  // test control, normally 0
   // synchronous scan for the first active item at idx, idx + grid, ...; result in ctrl->nx_*
   auto scan = [&](int idx) {
     TileItem ti = {0, 0};
@@ -358,7 +359,7 @@ rk4_2d_reg(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items,
     ctrl->item[b] = ctrl->nx_idx;
     ctrl->ti[b] = ti;
     fence_proxy_async_smem();
-    mbar_expect_tx(bar, (uint32_t)(G::STAGE_U + G::STAGE_P + G::DESC));
+    mbar_expect_tx(bar, (uint32_t)(G::STAGE_U + G::STAGE_P + G::DESC) + tx_extra);
     tma_load_2d(stage_u, maps + par, txi * G::TX - H, tyi * G::TY - H, bar);
     tma_load_2d(stage_p, maps + 2, txi * G::TX - H, tyi * G::TY - H, bar);
     bulk_load(desc + b, insts + ti.inst, (uint32_t)G::DESC, bar);

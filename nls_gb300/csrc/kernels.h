@@ -65,6 +65,9 @@ cudaError_t launch_2d_fused_tma(int K, int shape, const Inst2D* d_insts, const T
                                 int n_items, int j_step, int grid, cudaStream_t s);
 // 1 if a bounded tile wait expired since the last call (then cleared), 0 if not, -1 on error
 int tile_wait_timeout_read_clear(cudaStream_t s);
+// Test control: arm every tile barrier of the register-tile kernel for this many bytes more than
+// its copies deliver (0 = normal operation), on the current device.
+cudaError_t tile_tx_extra_set(unsigned bytes);
 cudaError_t launch_2d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,
                             void* acc, void* dst, double dt, const PhysD& ph, const Stencil2D& op,
                             cudaStream_t st);

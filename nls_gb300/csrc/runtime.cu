@@ -977,6 +977,11 @@ NLS_API int nls_batch_create(nls_ctx* ctx, int dtype, int count, const nls_probl
   return NLS_OK;
 }
 
+NLS_API int nls_test_set_tile_tx_extra(int device, unsigned extra_bytes) {
+  if (cudaSetDevice(device) != cudaSuccess) return NLS_ERR_CUDA;
+  return tile_tx_extra_set(extra_bytes) == cudaSuccess ? NLS_OK : NLS_ERR_CUDA;
+}
+
 NLS_API int nls_batch_set(nls_batch* b, int index, const void* pumping, const void* u0) {
   if (!b) return NLS_ERR_INVALID;
   nls_ctx* ctx = b->ctx;

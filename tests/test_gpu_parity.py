@@ -372,3 +372,22 @@ def test_2d_c64_register_tiles_small_and_ragged(gpu, oracle_lib, variant, order,
     want32 = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float32)
     got = _device_solve(gpu, s, iters, np.complex64, variant)
     assert rel(got, want32) <= 3e-5
+
+
+def test_tile_wait_timeout_is_reported_and_the_context_recovers(gpu, oracle_lib):
+    """A tile barrier armed for more bytes than its copies bring never completes: the bounded wait
+    gives up (about a second), the solve reports NLS_ERR_TIMEOUT, and the next solve is correct."""
+    from nls_gb300 import _lib, device
+    s = _spec_2d(152, 3)                          # 152 = multiple of 4: the TMA path
+    assert _lib.lib().nls_test_set_tile_tx_extra(0, 16) == _lib.NLS_OK
+    try:
+        # the device-pointer solve only enqueues; the context's synchronize reports the expiry
+        _device_solve(gpu, s, 1, np.complex64, 10)
+        with pytest.raises(_lib.NativeError) as err:
+            device.context(0).synchronize()
+        assert err.value.status == _lib.NLS_ERR_TIMEOUT
+    finally:
+        assert _lib.lib().nls_test_set_tile_tx_extra(0, 0) == _lib.NLS_OK
+    got = _device_solve(gpu, s, 40, np.complex64, 10)
+    want = oracle_lib.solve(s.dt, s.dx, 3, 40, s.pumping, s.coeffs, s.u0, dtype=np.float32)
+    assert rel(got, want) <= 3e-5
