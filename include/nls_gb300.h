@@ -172,8 +172,9 @@ int nls_pool_destroy(nls_pool* pool);
  * budget at start-up and may never grow it, host frameworks whose own caching allocator owns the
  * GPU's memory, and latency-critical loops that cannot pay for cudaMalloc / cudaFree, which can
  * synchronise the device and stall unrelated streams.  The call advances u_dev (n x n, in place)
- * by iters RK4 steps of the 2-D model with the same fused tile kernel as nls_solve_device, on the
- * caller's stream (NULL = the legacy default stream), with no cudaMalloc, cudaFree or other
+ * by iters RK4 steps of the 2-D model with a fused tile kernel of nls_solve_device (variant as
+ * there; by default the register-resident tile for complex64 and the 32x32 tile for complex128),
+ * on the caller's stream (NULL = the legacy default stream), with no cudaMalloc, cudaFree or other
  * allocating call: its scratch (the second state buffer, the descriptor and the tile list) is a
  * fixed file-scope device array of about 4 MiB, which every GPU that loads this library holds
  * until the process exits.  Limits: dim must be 2 and n * n <= NLS_NOALLOC_MAX_NODES (512 x 512),

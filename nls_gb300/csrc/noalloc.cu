@@ -5,9 +5,11 @@
 // all of its device memory up front and must never grow it, a host framework whose own caching
 // allocator owns the GPU's memory, or a latency-critical loop that cannot afford cudaMalloc /
 // cudaFree, which may synchronise the whole device and stall unrelated streams.
-// nls_solve_2d_noalloc() serves them: it runs the same fused tile kernel (rk4_2d_fused), but its
-// scratch -- the second state buffer of the ping-pong, the instance descriptor and the tile list
-// -- lives in one file-scope __device__ array of fixed size, so the call allocates nothing.
+// nls_solve_2d_noalloc() serves them: it runs a fused tile kernel of nls_solve_device (for
+// complex64 by default the same register-resident tile, rk4_2d_reg; for complex128 the 32x32
+// rk4_2d_fused tile, since the stage kernels nls_solve_device uses there need more scratch), but
+// its scratch -- the second state buffer of the ping-pong, the instance descriptor and the tile
+// list -- lives in one file-scope __device__ array of fixed size, so the call allocates nothing.
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -69,8 +71,8 @@ NLS_API int nls_solve_2d_noalloc(int dtype, const nls_problem* pr, int64_t iters
   Stencil2D op;
   if (host_stencil_2d(pr->order, pr->dx, &op)) return NLS_ERR_ORDER;
   // fused tile shape: the caller's choice if it names a fused tile this precision supports,
-  // otherwise 64x64 (complex64) or 32x32 (complex128)
-  int shape = dtype == NLS_C64 ? TILE_64x64 : TILE_32x32;
+  // otherwise the register-resident 64x96 tile (complex64) or the 32x32 tile (complex128)
+  int shape = dtype == NLS_C64 ? TILE_R64x96S : TILE_32x32;
   if (pr->variant > 0 && tile_supported(pr->variant, dtype)) shape = pr->variant;
   const int n = pr->n;
   const int tx = tile_out_x(shape, op.K), ty = tile_out_y(shape, op.K);

@@ -39,7 +39,8 @@ def _case(n, order, seed):
     return s
 
 
-@pytest.mark.parametrize("dtype,variant,tol", [(np.complex64, 1, 3e-5), (np.complex128, 3, 1e-10)])
+@pytest.mark.parametrize("dtype,variant,tol", [(np.complex64, 1, 3e-5), (np.complex64, 10, 3e-5),
+                                               (np.complex128, 3, 1e-10)])
 def test_noalloc_matches_solve_device_on_two_calls(env, dtype, variant, tol):
     torch, _lib = env
     from nls_gb300 import device
