@@ -193,7 +193,15 @@ __device__ __forceinline__ void reg_stage(float2 (&tX)[NJ], float2 (&tY)[NJ], fl
     }
     if (S < 4) {
       float2 vX, vY;
-      if (S == 3) {
+      // Next stage input u + q (u + 2 q before stage 4).  Packed or scalar by tile shape, as
+      // measured on the GB300: scalar is faster for strips of up to 10 rows and at order 5,
+      // packed for 12-row strips at order 3 (the register allocation differs, not the work).
+      constexpr bool kScalarUpdate = NJ <= 10 || K == 2;
+      if (kScalarUpdate) {
+        const float m = S == 3 ? 2.f : 1.f;
+        vX = f2(__fmaf_rn(m, kX.x, uX[j].x), __fmaf_rn(m, kX.y, uX[j].y));
+        vY = f2(__fmaf_rn(m, kY.x, uY[j].x), __fmaf_rn(m, kY.y, uY[j].y));
+      } else if (S == 3) {
         vX = fma2(c.two, kX, uX[j]);
         vY = fma2(c.two, kY, uY[j]);
       } else {
