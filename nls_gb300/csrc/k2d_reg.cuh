@@ -216,8 +216,14 @@ __device__ __forceinline__ void reg_stage(float2 (&tX)[NJ], float2 (&tY)[NJ], fl
       nX[j] = vX;
       nY[j] = vY;
     } else {
-      uX[j] = fma2(c.third, aX[j], uX[j]);
-      uY[j] = fma2(c.third, aY[j], uY[j]);
+      if (NJ <= 10 || K == 2) {  // scalar for the same shapes as the stage-input update
+        const float th = 1.f / 3.f;
+        uX[j] = f2(__fmaf_rn(th, aX[j].x, uX[j].x), __fmaf_rn(th, aX[j].y, uX[j].y));
+        uY[j] = f2(__fmaf_rn(th, aY[j].x, uY[j].x), __fmaf_rn(th, aY[j].y, uY[j].y));
+      } else {
+        uX[j] = fma2(c.third, aX[j], uX[j]);
+        uY[j] = fma2(c.third, aY[j], uY[j]);
+      }
     }
   }
   if (S < 4) {
