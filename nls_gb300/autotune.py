@@ -179,9 +179,10 @@ def tune_mix(specs, dtype=np.complex64, steps: int = 32, device: int = 0):
 def apply(specs, dtype=np.complex64, device: int = 0, mode: str = "batch"):
     """Set each Spec.variant from the tuned choice; returns the choices.
 
-    1-D specs: the fastest cluster size of their size bucket.  2-D specs: per size bucket in
-    ``single`` mode; in ``batch`` mode one shape per stencil order, timed on the batch itself
-    (``tune_mix``), unless the per-bucket choices together time faster on it."""
+    1-D specs: the fastest cluster size of their size bucket; in ``batch`` mode then refined on
+    the batch itself.  2-D specs: per size bucket in ``single`` mode; in ``batch`` mode one shape
+    per stencil order, timed on the batch itself (``tune_mix``), unless the per-bucket choices
+    together time faster on it."""
     memo = {}
     out = {}
     two_d = {}
@@ -193,8 +194,6 @@ def apply(specs, dtype=np.complex64, device: int = 0, mode: str = "batch"):
         if k not in memo:
             memo[k] = tune(s.dim, s.n, s.order, dtype=dtype, device=device, mode=mode)
         s.variant = memo[k]
-    for (d, o, b), v in sorted(memo.items()):
-        out[f"{d}d/o{o}/n<={b}"] = v
     for order, group in sorted(two_d.items()):
         best, times = tune_mix(group, dtype=dtype, device=device)
         # per-bucket choices as one more candidate
@@ -216,6 +215,33 @@ def apply(specs, dtype=np.complex64, device: int = 0, mode: str = "batch"):
             for s in group:
                 s.variant = best
             out[f"2d/o{order}/mix"] = best
+    # 1-D in a batch: the per-size choices above maximise the throughput of a GPU full of copies
+    # of one grid, which favours wide clusters; inside a mix the 1-D grids share the SMs with the
+    # 2-D steps and fewer CTAs per grid can cost less SM time.  One pass of coordinate descent on
+    # the batch itself, largest size bucket first, over that bucket's cluster sizes.
+    if mode == "batch" and any(s.dim == 1 for s in specs):
+        keys = sorted({(s.order, bucket(s.n)) for s in specs if s.dim == 1}, key=lambda k: -k[1])
+        best_t = _time_mix_assigned([copy.copy(s) for s in specs], dtype, 32, device)
+        for order, b in keys:
+            group = [s for s in specs if s.dim == 1 and s.order == order and bucket(s.n) == b]
+            for v in candidates(1, dtype, b):
+                if v == 0 or v == group[0].variant:
+                    continue
+                trial = [copy.copy(s) for s in specs]
+                for t in trial:
+                    if t.dim == 1 and t.order == order and bucket(t.n) == b:
+                        t.variant = v
+                try:
+                    t_v = _time_mix_assigned(trial, dtype, 32, device)
+                except ValueError:
+                    continue
+                if t_v < best_t:
+                    best_t = t_v
+                    for s in group:
+                        s.variant = v
+                    memo[(1, order, b)] = v
+    for (d, o, b), v in sorted(memo.items()):
+        out[f"{d}d/o{o}/n<={b}"] = v
     return out
 
 

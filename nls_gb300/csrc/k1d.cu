@@ -14,6 +14,7 @@
 
 #include "kernels.h"
 #include "nls_common.cuh"
+#include "k1d_reg.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -571,8 +572,37 @@ static cudaError_t launch_res_npt(const Inst1D* d, int count, int cl, int seg_ca
   }
 }
 
+// Complex64 on one CTA per grid: the register-resident kernel, NPT consecutive nodes per thread
+// (a power of two >= K, at most 8) on up to 512 threads.
+template <int K>
+static cudaError_t launch_reg1d(const Inst1D* d, int count, int seg_cap, cudaStream_t s, bool prepare_only) {
+  int npt = 1;
+  while (npt < K) npt *= 2;
+  while (npt * 512 < seg_cap) npt *= 2;
+  if (npt > 8) return cudaErrorInvalidValue;
+  int nt = (seg_cap + npt - 1) / npt;
+  nt = ((nt + 31) / 32) * 32;
+  const size_t smem = (size_t)2 * (nt / 32) * 2 * K * sizeof(float2);
+  if (prepare_only) return cudaSuccess;
+  switch (npt) {
+    case 1: if (K <= 1) { rk4_1d_reg<(K <= 1 ? K : 1), 1><<<count, nt, smem, s>>>(d); return cudaGetLastError(); }
+            return cudaErrorInvalidValue;
+    case 2: if (K <= 2) { rk4_1d_reg<(K <= 2 ? K : 2), 2><<<count, nt, smem, s>>>(d); return cudaGetLastError(); }
+            return cudaErrorInvalidValue;
+    case 4: rk4_1d_reg<K, 4><<<count, nt, smem, s>>>(d); return cudaGetLastError();
+    case 8: rk4_1d_reg<K, 8><<<count, nt, smem, s>>>(d); return cudaGetLastError();
+  }
+  return cudaErrorInvalidValue;
+}
+
 static cudaError_t dispatch_res(int dtype, int K, const Inst1D* d_insts, int count, int cl,
                                 int seg_cap, cudaStream_t s, bool prepare_only) {
+  if (dtype == NLS_C64 && cl == 1) {
+    if (K == 1) return launch_reg1d<1>(d_insts, count, seg_cap, s, prepare_only);
+    if (K == 2) return launch_reg1d<2>(d_insts, count, seg_cap, s, prepare_only);
+    if (K == 3) return launch_reg1d<3>(d_insts, count, seg_cap, s, prepare_only);
+    return cudaErrorInvalidValue;
+  }
   if (dtype == NLS_C128) {
     if (K == 1) return launch_res_npt<double, 1>(d_insts, count, cl, seg_cap, s, prepare_only);
     if (K == 2) return launch_res_npt<double, 2>(d_insts, count, cl, seg_cap, s, prepare_only);

@@ -104,6 +104,20 @@ template <typename T> __host__ __device__ inline Cross<T> cross_from(const Stenc
   return c;
 }
 
+// Packed FP32x2 arithmetic on node pairs or (re, im) pairs (Blackwell FADD2 / FMUL2 / FFMA2).
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+// Approximate reciprocal (PTX rcp.approx.ftz.f32, relative error about one unit in the last
+// place): the reservoir quotient of the register-resident complex64 kernels.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // Warp + block reduction of NV doubles (fixed order, deterministic).
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double* smem /* >= 32*NV */) {
