@@ -250,28 +250,18 @@ def run_cpu(args):
 
 # ------------------------------------------------------------------ GPU legs
 
-def pinned_fields(specs, ctype, rtype):
-    """Per-instance pump, initial-state and output arrays in one pinned (page-locked) host block,
-    laid out as the C ABI reads them (Fortran order in 2-D), inputs filled from the specs."""
+def pinned_fields(b, specs):
+    """The batch's pumps, initial states and outputs as three pinned (page-locked) host blocks in
+    the batch's packed layout (``BatchSolver.layout``), inputs filled from the specs; returns the
+    blocks and the per-instance views of the output block."""
     import torch
-    sizes = []
-    for s in specs:
-        sizes += [s.nodes * np.dtype(rtype).itemsize, s.nodes * np.dtype(ctype).itemsize,
-                  s.nodes * np.dtype(ctype).itemsize]
-    offs = np.concatenate([[0], np.cumsum([(b + 255) // 256 * 256 for b in sizes])])
-    block = torch.empty(int(offs[-1]), dtype=torch.uint8, pin_memory=True).numpy()
-    views = []
-    for k, s in enumerate(specs):
-        shape = (s.n, s.n) if s.dim == 2 else (s.n,)
-        order = "F" if s.dim == 2 else "C"
-        for j, dt in enumerate((rtype, ctype, ctype)):
-            o = int(offs[3 * k + j])
-            views.append(np.ndarray(shape, dtype=dt, buffer=block, offset=o, order=order))
-    P, U, O = views[0::3], views[1::3], views[2::3]
-    for s, p, u in zip(specs, P, U):
+    _, _, pb, sb = b.layout()
+    blocks = [torch.empty(int(nb), dtype=torch.uint8, pin_memory=True).numpy() for nb in (pb, sb, sb)]
+    hP, hU, hO = blocks
+    for s, p, u in zip(specs, b.packed_views(hP, "pump"), b.packed_views(hU, "state")):
         p[...] = np.asarray(s.pumping)
         u[...] = np.asarray(s.u0)
-    return P, U, O
+    return hP, hU, hO
 
 
 def run_grid(args):
@@ -527,23 +517,27 @@ def run_ours(args):
 
     # ---- end to end through the host-buffer C ABI: upload u0 and P from pinned host memory,
     # solve, download every state into pinned host memory
-    h2d = sum(s.nodes * (8 + 4) for s in specs)
-    d2h = sum(s.nodes * 8 for s in specs)
-    hP, hU, hO = pinned_fields(specs, np.complex64, np.float32)
+    hP, hU, hO = pinned_fields(b, specs)
+    h2d, d2h = hP.nbytes + hU.nbytes, hO.nbytes   # the copied blocks, 256-byte padding included
     e2e_times = []
-    for rep in range(max(1, min(args.steps, 2))):
+    for rep in range(1 + max(1, min(args.steps, 3))):   # the first pass is an untimed warm-up
         ctx = b.ctx
         ctx.synchronize()
         t0 = time.perf_counter()
-        for i in range(len(specs)):
-            b.set(i, hP[i], hU[i])
+        b.set_packed(hP, hU)
         b.run(SOLVE_STEPS)
-        for i in range(len(specs)):
-            b.get(i, out=hO[i])
-        e2e_times.append(time.perf_counter() - t0)
+        b.get_packed(hO)
+        if rep:
+            e2e_times.append(time.perf_counter() - t0)
+    outs = b.packed_views(hO, "state")
+    for i in (0, len(specs) // 2, len(specs) - 1):   # the packed download is the batch's state
+        if not np.array_equal(outs[i], b.get(i)):
+            raise RuntimeError(f"packed download differs from nls_batch_get for instance {i}")
+    del outs
     e2e = float(total_nodes) * SOLVE_STEPS / float(np.mean(e2e_times))
     result["e2e"] = {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                     "path": "nls_batch_set (pinned host u0, P) -> nls_batch_run(5000) -> nls_batch_get (pinned host u)"}
+                     "path": "nls_batch_set_packed (pinned host blocks of every P and u0) -> nls_batch_run(5000) -> "
+                             "nls_batch_get_packed (pinned host block of every u)"}
     del hP, hU, hO
 
     # ---- served stream (continuous batching) p50/p99

@@ -139,6 +139,21 @@ int nls_batch_set(nls_batch* batch, int index, const void* pumping, const void* 
 int nls_batch_run(nls_batch* batch, int64_t steps);
 /* Copy instance index's current state to a host buffer; blocks until written. */
 int nls_batch_get(nls_batch* batch, int index, void* u);
+/* The same for count instances first .. first+count-1 (pumping[k], u0[k] / u[k] belong to
+ * instance first+k): every copy is queued on the context's stream and the call synchronizes once,
+ * instead of once per instance.  Pinned host buffers make the copies asynchronous DMA. */
+int nls_batch_set_many(nls_batch* batch, int first, int count, const void* const* pumping,
+                       const void* const* u0);
+int nls_batch_get_many(nls_batch* batch, int first, int count, void* const* u);
+/* Packed host layout of a batch: every pump in one block and every state in another, instance
+ * k's at byte offset pump_offsets[k] / state_offsets[k] (instance order, each padded to 256
+ * bytes; the arrays hold count entries, any output may be NULL), the blocks pump_bytes and
+ * state_bytes long.  The batch keeps its device fields in the same layout, so set_packed and
+ * get_packed move the whole batch in a few large copies, one wait each. */
+int nls_batch_layout(nls_batch* batch, int64_t* pump_offsets, int64_t* state_offsets,
+                     int64_t* pump_bytes, int64_t* state_bytes);
+int nls_batch_set_packed(nls_batch* batch, const void* pumping, const void* u0);
+int nls_batch_get_packed(nls_batch* batch, void* u);
 /* Device pointers of instance index's current state and pump (valid until the next run). */
 int nls_batch_state(nls_batch* batch, int index, void** u_dev, const void** pumping_dev);
 /* Kernel launches one run(steps) issues, and nodes summed over instances. */

@@ -79,6 +79,11 @@ SIGNATURES = {
     "nls_batch_set": (_i, [_p, _i, _p, _p]),
     "nls_batch_run": (_i, [_p, _i64]),
     "nls_batch_get": (_i, [_p, _i, _p]),
+    "nls_batch_set_many": (_i, [_p, _i, _i, _p, _p]),
+    "nls_batch_get_many": (_i, [_p, _i, _i, _p]),
+    "nls_batch_layout": (_i, [_p, _p, _p, _p, _p]),
+    "nls_batch_set_packed": (_i, [_p, _p, _p]),
+    "nls_batch_get_packed": (_i, [_p, _p]),
     "nls_batch_state": (_i, [_p, _i, ctypes.POINTER(_p), ctypes.POINTER(_p)]),
     "nls_batch_info": (_i, [_p, _i64, _pi64, _pi64]),
     "nls_batch_destroy": (_i, [_p]),

@@ -512,6 +512,8 @@ struct nls_batch {
   char* mem = nullptr;       // one allocation for states, pumps, descriptors
   size_t mem_bytes = 0;
   int parity = 0;            // common parity of the 2-D fused instances
+  std::vector<size_t> poff, soff;  // packed host layout: pump and state byte offsets per instance
+  size_t pump_bytes = 0, state_bytes = 0;
   std::map<int64_t, cudaGraphExec_t> graphs;
   std::mutex mu;
 };
@@ -562,12 +564,29 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
         b->g2[M.group].idx.push_back(i);
       }
     }
-    const size_t cb = align256(M.N * csize(dtype)), pb = align256(M.N * rsize(dtype));
-    offs[4 * i + 0] = off; off += cb;
-    offs[4 * i + 1] = off; if (M.kind == 2) off += cb;
-    offs[4 * i + 2] = off; off += pb;
-    offs[4 * i + 3] = off; if (M.kind == 3 || M.kind == 4) off += 3 * cb;
   }
+  // states and pumps field by field -- every pump, every state, the second state buffers of the
+  // fused 2-D instances, the unfused stage buffers -- each instance padded to 256 bytes, so the pump
+  // and state blocks have the packed host layout of nls_batch_set_packed / nls_batch_get_packed
+  b->poff.resize(count);
+  b->soff.resize(count);
+  for (int i = 0; i < count; ++i) {
+    offs[4 * i + 2] = off;
+    b->poff[i] = off;
+    off += align256(b->m[i].N * rsize(dtype));
+  }
+  b->pump_bytes = off;
+  const size_t state_base = off;
+  for (int i = 0; i < count; ++i) {
+    offs[4 * i + 0] = off;
+    b->soff[i] = off - state_base;
+    off += align256(b->m[i].N * csize(dtype));
+  }
+  b->state_bytes = off - state_base;
+  for (int i = 0; i < count; ++i)
+    if (b->m[i].kind == 2) { offs[4 * i + 1] = off; off += align256(b->m[i].N * csize(dtype)); }
+  for (int i = 0; i < count; ++i)
+    if (b->m[i].kind == 3 || b->m[i].kind == 4) { offs[4 * i + 3] = off; off += 3 * align256(b->m[i].N * csize(dtype)); }
   // descriptors
   std::vector<size_t> g1off(b->g1.size()), g2off(b->g2.size()), g2items(b->g2.size()), g2maps;
   for (size_t g = 0; g < b->g1.size(); ++g) { g1off[g] = off; off += align256(sizeof(Inst1D) * b->g1[g].idx.size()); }
@@ -1039,6 +1058,111 @@ NLS_API int nls_batch_get(nls_batch* b, int index, void* u) {
   CK(ctx, cudaSetDevice(ctx->device));
   const Member& M = b->m[index];
   CK(ctx, cudaMemcpyAsync(u, M.u[M.parity], M.N * csize(b->dtype), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return NLS_OK;
+}
+
+NLS_API int nls_batch_set_many(nls_batch* b, int first, int count, const void* const* pumping,
+                               const void* const* u0) {
+  if (!b) return NLS_ERR_INVALID;
+  nls_ctx* ctx = b->ctx;
+  std::lock_guard<std::mutex> lk(b->mu);
+  if (first < 0 || count < 0 || first > (int)b->m.size() - count || (count && (!pumping || !u0)))
+    return fail(ctx, NLS_ERR_INVALID, "bad arguments");
+  for (int k = 0; k < count; ++k)
+    if (!pumping[k] || !u0[k]) return fail(ctx, NLS_ERR_INVALID, "null host buffer");
+  CK(ctx, cudaSetDevice(ctx->device));
+  for (int k = 0; k < count; ++k) {
+    Member& M = b->m[first + k];
+    CK(ctx, cudaMemcpyAsync(M.P, pumping[k], M.N * rsize(b->dtype), cudaMemcpyHostToDevice, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(M.u[M.parity], u0[k], M.N * csize(b->dtype), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return NLS_OK;
+}
+
+NLS_API int nls_batch_get_many(nls_batch* b, int first, int count, void* const* u) {
+  if (!b) return NLS_ERR_INVALID;
+  nls_ctx* ctx = b->ctx;
+  std::lock_guard<std::mutex> lk(b->mu);
+  if (first < 0 || count < 0 || first > (int)b->m.size() - count || (count && !u))
+    return fail(ctx, NLS_ERR_INVALID, "bad arguments");
+  for (int k = 0; k < count; ++k)
+    if (!u[k]) return fail(ctx, NLS_ERR_INVALID, "null host buffer");
+  CK(ctx, cudaSetDevice(ctx->device));
+  for (int k = 0; k < count; ++k) {
+    const Member& M = b->m[first + k];
+    CK(ctx, cudaMemcpyAsync(u[k], M.u[M.parity], M.N * csize(b->dtype), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return NLS_OK;
+}
+
+NLS_API int nls_batch_layout(nls_batch* b, int64_t* pump_offsets, int64_t* state_offsets,
+                             int64_t* pump_bytes, int64_t* state_bytes) {
+  if (!b) return NLS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(b->mu);
+  for (size_t i = 0; i < b->m.size(); ++i) {
+    if (pump_offsets) pump_offsets[i] = (int64_t)b->poff[i];
+    if (state_offsets) state_offsets[i] = (int64_t)b->soff[i];
+  }
+  if (pump_bytes) *pump_bytes = (int64_t)b->pump_bytes;
+  if (state_bytes) *state_bytes = (int64_t)b->state_bytes;
+  return NLS_OK;
+}
+
+namespace {
+// Merges copies whose source and destination both continue where the previous one ended: within
+// one packed block that are consecutive instances, so a whole batch moves in a few large copies.
+struct CopyRun {
+  nls_ctx* ctx;
+  cudaMemcpyKind kind;
+  char* dst = nullptr;
+  const char* src = nullptr;
+  size_t bytes = 0;
+  cudaError_t add(char* d, const char* s, size_t n) {
+    if (bytes && d == dst + bytes && s == src + bytes) { bytes += n; return cudaSuccess; }
+    cudaError_t e = flush();
+    dst = d; src = s; bytes = n;
+    return e;
+  }
+  cudaError_t flush() {
+    cudaError_t e = bytes ? cudaMemcpyAsync(dst, src, bytes, kind, ctx->stream) : cudaSuccess;
+    bytes = 0;
+    return e;
+  }
+};
+}  // namespace
+
+NLS_API int nls_batch_set_packed(nls_batch* b, const void* pumping, const void* u0) {
+  if (!b) return NLS_ERR_INVALID;
+  nls_ctx* ctx = b->ctx;
+  std::lock_guard<std::mutex> lk(b->mu);
+  if (!pumping || !u0) return fail(ctx, NLS_ERR_INVALID, "bad arguments");
+  CK(ctx, cudaSetDevice(ctx->device));
+  if (b->pump_bytes) CK(ctx, cudaMemcpyAsync(b->mem, pumping, b->pump_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  CopyRun run{ctx, cudaMemcpyHostToDevice};
+  for (size_t i = 0; i < b->m.size(); ++i) {
+    const Member& M = b->m[i];
+    CK(ctx, run.add(M.u[M.parity], static_cast<const char*>(u0) + b->soff[i], align256(M.N * csize(b->dtype))));
+  }
+  CK(ctx, run.flush());
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return NLS_OK;
+}
+
+NLS_API int nls_batch_get_packed(nls_batch* b, void* u) {
+  if (!b) return NLS_ERR_INVALID;
+  nls_ctx* ctx = b->ctx;
+  std::lock_guard<std::mutex> lk(b->mu);
+  if (!u) return fail(ctx, NLS_ERR_INVALID, "bad arguments");
+  CK(ctx, cudaSetDevice(ctx->device));
+  CopyRun run{ctx, cudaMemcpyDeviceToHost};
+  for (size_t i = 0; i < b->m.size(); ++i) {
+    const Member& M = b->m[i];
+    CK(ctx, run.add(static_cast<char*>(u) + b->soff[i], M.u[M.parity], align256(M.N * csize(b->dtype))));
+  }
+  CK(ctx, run.flush());
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   return NLS_OK;
 }

@@ -9,6 +9,8 @@ Tolerances (relative L2 over the whole field):
 
 import os
 
+import copy
+
 import numpy as np
 import pytest
 
@@ -286,6 +288,75 @@ def test_batch_matches_single_solves(gpu, dtype, shape2d):
         got = b.get(i)
         want = _device_solve(gpu, s, 77, dtype, s.variant)
         assert np.array_equal(got, want.astype(got.dtype)), i
+
+
+def test_batch_set_get_many_match_per_instance(gpu):
+    """The one-wait bulk upload and download equal per-instance set/get bit for bit, on a
+    sub-range and on the whole batch."""
+    from nls_gb300.batch import BatchSolver
+    specs = _mixed_specs(np.complex64)
+    a = BatchSolver(specs, dtype=np.complex64)
+    b = BatchSolver([copy.copy(s) for s in specs], dtype=np.complex64)
+    rng = np.random.default_rng(5)
+    newP, newU = [], []
+    for s in specs:
+        shape = (s.n, s.n) if s.dim == 2 else (s.n,)
+        newP.append(rng.uniform(0.5, 2.0, shape).astype(np.float32))
+        newU.append((rng.normal(size=shape) + 1j * rng.normal(size=shape)).astype(np.complex64) * 0.1)
+    lo, hi = 1, len(specs) - 1
+    for i in range(lo, hi):
+        a.set(i, newP[i], newU[i])
+    b.set_many(newP[lo:hi], newU[lo:hi], first=lo)
+    a.run(33)
+    b.run(33)
+    whole = b.get_many()
+    part = b.get_many([np.empty_like(whole[i], order="F" if specs[i].dim == 2 else "C")
+                       for i in range(lo, hi)], first=lo)
+    for i in range(len(specs)):
+        want = a.get(i)
+        assert np.array_equal(whole[i], want), i
+        if lo <= i < hi:
+            assert np.array_equal(part[i - lo], want), i
+    with pytest.raises(ValueError):
+        b.get_many(first=len(specs) - 1, outs=[None, None])
+
+
+@pytest.mark.parametrize("steps", [34, 33])   # 2-D states end in the first / second buffer
+def test_batch_packed_layout_matches_per_instance(gpu, steps):
+    """Packed blocks: offsets in instance order, 256-byte aligned and padded; the packed upload and
+    download equal per-instance set/get bit for bit, whichever state buffer is current."""
+    from nls_gb300.batch import BatchSolver
+    specs = _mixed_specs(np.complex64)
+    a = BatchSolver(specs, dtype=np.complex64)
+    b = BatchSolver([copy.copy(s) for s in specs], dtype=np.complex64)
+    po, so, pb, sb = b.layout()
+    for offs, total, item in ((po, pb, 4), (so, sb, 8)):
+        ends = [o + s.nodes * item for o, s in zip(offs, specs)]
+        assert offs[0] == 0 and all(o % 256 == 0 for o in offs)
+        assert all(e <= o2 for e, o2 in zip(ends[:-1], offs[1:])) and ends[-1] <= total
+        assert all(o2 - e < 256 for e, o2 in zip(ends[:-1], list(offs[1:]))) and total - ends[-1] < 256
+    rng = np.random.default_rng(9)
+    hP, hU = np.zeros(pb, np.uint8), np.zeros(sb, np.uint8)
+    for i, (p, u) in enumerate(zip(b.packed_views(hP, "pump"), b.packed_views(hU, "state"))):
+        p[...] = rng.uniform(0.5, 2.0, p.shape)
+        u[...] = (rng.normal(size=u.shape) + 1j * rng.normal(size=u.shape)) * 0.1
+        a.set(i, p, u)
+    b.set_packed(hP, hU)
+    a.run(steps)
+    b.run(steps)
+    out = b.get_packed()
+    for i, got in enumerate(b.packed_views(out, "state")):
+        assert np.array_equal(got, a.get(i)), i
+    # a second packed upload over states that sit in the second buffer, then one more run
+    b.set_packed(hP, hU)
+    for i, (p, u) in enumerate(zip(b.packed_views(hP, "pump"), b.packed_views(hU, "state"))):
+        a.set(i, p, u)
+    a.run(5)
+    b.run(5)
+    for i, got in enumerate(b.packed_views(b.get_packed(), "state")):
+        assert np.array_equal(got, a.get(i)), i
+    with pytest.raises(ValueError):
+        b.set_packed(hP[:-1], hU)
 
 
 def test_pool_same_alone_and_in_the_mix(gpu):
