@@ -519,16 +519,22 @@ def run_ours(args):
     # solve, download every state into pinned host memory
     hP, hU, hO = pinned_fields(b, specs)
     h2d, d2h = hP.nbytes + hU.nbytes, hO.nbytes   # the copied blocks, 256-byte padding included
-    e2e_times = []
-    for rep in range(1 + max(1, min(args.steps, 3))):   # the first pass is an untimed warm-up
-        ctx = b.ctx
-        ctx.synchronize()
-        t0 = time.perf_counter()
-        b.set_packed(hP, hU)
-        b.run(SOLVE_STEPS)
-        b.get_packed(hO)
-        if rep:
-            e2e_times.append(time.perf_counter() - t0)
+    e2e_times, phases = [], []
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk_e2e:
+        for rep in range(1 + max(1, min(args.steps, 3))):   # the first pass is an untimed warm-up
+            b.ctx.synchronize()
+            t0 = time.perf_counter()
+            b.set_packed(hP, hU)
+            t1 = time.perf_counter()
+            r0.record(ext)
+            b.run(SOLVE_STEPS)
+            r1.record(ext)
+            b.get_packed(hO)
+            t2 = time.perf_counter()
+            if rep:
+                e2e_times.append(t2 - t0)
+                phases.append(((t1 - t0) * 1e3, r0.elapsed_time(r1), (t2 - t0) * 1e3))
     outs = b.packed_views(hO, "state")
     for i in (0, len(specs) // 2, len(specs) - 1):   # the packed download is the batch's state
         if not np.array_equal(outs[i], b.get(i)):
@@ -537,7 +543,9 @@ def run_ours(args):
     e2e = float(total_nodes) * SOLVE_STEPS / float(np.mean(e2e_times))
     result["e2e"] = {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                      "path": "nls_batch_set_packed (pinned host blocks of every P and u0) -> nls_batch_run(5000) -> "
-                             "nls_batch_get_packed (pinned host block of every u)"}
+                             "nls_batch_get_packed (pinned host block of every u)",
+                     "ms_upload_run_total": [[round(x, 2) for x in ph] for ph in phases],
+                     "clocks": clk_e2e.summary()}
     del hP, hU, hO
 
     # ---- served stream (continuous batching) p50/p99
