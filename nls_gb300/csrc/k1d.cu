@@ -573,13 +573,17 @@ static cudaError_t launch_res_npt(const Inst1D* d, int count, int cl, int seg_ca
 }
 
 // Complex64 on one CTA per grid: the register-resident kernel, NPT consecutive nodes per thread
-// (a power of two >= K, at most 8) on up to 512 threads.
+// (a power of two >= K, at most 8) on up to 512 threads.  One grid alone takes the smallest NPT
+// that fits (most threads: the shortest step); a launch of many grids takes NPT = 8, the fewest
+// threads per grid, so that small grids share an SM and each node costs the least SM time (fewer
+// halo exchanges and barrier waits per node) -- in a batch the GPU's throughput is what counts.
 template <int K>
 static cudaError_t launch_reg1d(const Inst1D* d, int count, int seg_cap, cudaStream_t s, bool prepare_only) {
   int npt = 1;
   while (npt < K) npt *= 2;
   while (npt * 512 < seg_cap) npt *= 2;
-  if (npt > 8) return cudaErrorInvalidValue;
+  if (count > 1) npt = 8;
+  if (npt > 8 || npt < K) return cudaErrorInvalidValue;
   int nt = (seg_cap + npt - 1) / npt;
   nt = ((nt + 31) / 32) * 32;
   const size_t smem = (size_t)2 * (nt / 32) * 2 * K * sizeof(float2);
