@@ -16,7 +16,9 @@ Two objectives: ``mode="single"`` times one solve of the size (latency of a lone
 what a batched or served mix cares about: a shape with less halo recomputation wins there even
 when it exposes fewer tiles per grid).  For a batch, ``apply`` also times the batch's own 2-D
 specs under one shared shape (one persistent launch per step instead of one per shape) against
-the per-size choices and keeps the faster.  Per-size results are cached per GPU name in a JSON
+the per-size choices and keeps the faster, then refines the 1-D cluster sizes on the batch itself
+(one pass of coordinate descent over the size buckets, largest first): inside a mix the 1-D grids
+share the GPU with the 2-D steps, so the fewest CTAs per grid often cost the batch least.  Per-size results are cached per GPU name in a JSON
 file (``NLS_GB300_TUNE_CACHE`` or ``~/.cache/nls_gb300/autotune.json``); ``apply(specs, dtype,
 mode)`` fills ``Spec.variant``.  Timings use CUDA events on the library's stream.
 """

@@ -187,3 +187,42 @@ def test_autotune_assign_maps_choices_to_other_specs():
     choices["2d/o3/mix"] = 12
     autotune.assign(specs, choices)
     assert all(s.variant == (4 if s.dim == 1 else 12) for s in specs)
+
+
+def test_autotune_batch_refines_1d_cluster_sizes_on_the_batch(monkeypatch):
+    """Batch mode starts the 1-D specs from the per-size choice and keeps, per size bucket, the
+    cluster size that times fastest on the whole batch (fake timings, no GPU)."""
+    from nls_gb300 import autotune
+    from nls_gb300 import workloads as w
+    specs = [w.mix_instance(i, 1, with_data=False) for i in range(40)] + \
+            [w.mix_instance(100 + i, 2, with_data=False) for i in range(3)]
+    assert any(s.n > 4096 for s in specs if s.dim == 1) and any(s.n <= 4096 for s in specs if s.dim == 1)
+
+    def best(n):
+        return 1 if n <= 4096 else 4
+
+    def cost(s):
+        order = [1, 2, 4, 8, 16] if s.n <= 4096 else [4, 2, 8, 16]
+        return 1.0 + order.index(s.variant) if s.variant in order else 100.0
+
+    calls = []
+    monkeypatch.setattr(autotune, "tune", lambda dim, n, order, **kw: 16 if dim == 1 else 12)
+    monkeypatch.setattr(autotune, "tune_mix", lambda group, **kw: (12, {12: 1.0}))
+
+    def fake_time(trial, dtype, steps, device):
+        calls.append(1)
+        return 50.0 + sum(cost(t) for t in trial if t.dim == 1)
+
+    monkeypatch.setattr(autotune, "_time_mix_assigned", fake_time)
+    out = autotune.apply(specs, dtype=np.complex64, mode="batch")
+    for s in specs:
+        if s.dim == 1:
+            assert s.variant == best(s.n), (s.n, s.variant)
+            assert out[f"1d/o{s.order}/n<={autotune.bucket(s.n)}"] == s.variant
+        else:
+            assert s.variant == 12
+    assert calls
+    # single mode keeps the per-size choice
+    single = [w.mix_instance(i, 1, with_data=False) for i in range(5)]
+    autotune.apply(single, dtype=np.complex64, mode="single")
+    assert all(s.variant == 16 for s in single)
