@@ -187,18 +187,23 @@ int nls_pool_destroy(nls_pool* pool);
  * budget at start-up and may never grow it, host frameworks whose own caching allocator owns the
  * GPU's memory, and latency-critical loops that cannot pay for cudaMalloc / cudaFree, which can
  * synchronise the device and stall unrelated streams.  The call advances u_dev (n x n, in place)
- * by iters RK4 steps of the 2-D model with a fused tile kernel of nls_solve_device (variant as
- * there; by default the register-resident tile for complex64 and the 32x32 tile for complex128),
- * on the caller's stream (NULL = the legacy default stream), with no cudaMalloc, cudaFree or other
+ * by iters RK4 steps of the 2-D model with a fused tile kernel of nls_solve_device, on the
+ * caller's stream (NULL = the legacy default stream), with no cudaMalloc, cudaFree or other
  * allocating call: its scratch (the second state buffer, the descriptor and the tile list) is a
  * fixed file-scope device array of about 4 MiB, which every GPU that loads this library holds
- * until the process exits.  Limits: dim must be 2 and n * n <= NLS_NOALLOC_MAX_NODES (512 x 512),
- * otherwise NLS_ERR_TOO_LARGE.  The first call on a device resolves the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call before any stream
- * capture.  Every call shares the one array and it keeps the last call's contents (nothing in it
- * needs to start at zero: the first step overwrites every node it later reads), so calls that
- * overlap on the GPU -- on different streams or threads -- race; serialise them.  Returns after
- * enqueueing the work (no host synchronisation). */
+ * until the process exits.  variant: -1 = the register-resident 64x96 tile (complex64) or the
+ * 32x32 tile (complex128); otherwise a fused tile variant of nls_problem that the precision
+ * supports (variant 0, the unfused stage kernels, and unsupported variants: NLS_ERR_INVALID).
+ * The tile kernels run in their plain-load form, which has no copy barrier and so no bounded
+ * wait that could expire.  The descriptor and tile list are written into the array by a kernel
+ * on the caller's stream; no host memory is read after the call returns.  Limits: dim must be 2
+ * and n * n <= NLS_NOALLOC_MAX_NODES (512 x 512), otherwise NLS_ERR_TOO_LARGE.  The first call
+ * in a CUDA context resolves the array's device address in that context (cudaGetSymbolAddress,
+ * with that context's device current) and caches it per context; make that first call before
+ * any stream capture.  Every call shares the one array and it keeps the last call's contents
+ * (nothing in it needs to start at zero: the first step overwrites every node it later reads),
+ * so calls that overlap on the GPU -- on different streams or threads -- race; serialise them.
+ * Returns after enqueueing the work (no host synchronisation). */
 #define NLS_NOALLOC_MAX_NODES 262144
 int nls_solve_2d_noalloc(int dtype, const nls_problem* problem, int64_t iters,
                          const void* pumping_dev, void* u_dev, void* stream);

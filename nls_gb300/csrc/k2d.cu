@@ -14,8 +14,11 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "kernels.h"
 #include "nls_common.cuh"
@@ -150,8 +153,6 @@ __device__ __forceinline__ void tile_stage(const typename C2<T>::type* __restric
 
 // ---- TMA / mbarrier helpers (inline PTX, sm_90+ forms valid on sm_103a)
 
-// Set when a bounded wait on a tile copy gives up; read and cleared by the host.
-__device__ int g_tile_wait_timeout = 0;
 // Extra bytes the register-tile kernel arms its tile barrier for (0 in normal operation): a test
 // control that makes the bounded wait expire without any fault.
 __device__ unsigned g_tile_tx_extra = 0;
@@ -197,13 +198,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 }  // namespace nlsg
 
 #include "k2d_reg.cuh"
+#include "k2d_stream.cuh"
 
 namespace nlsg {
 
 template <typename T, int K, int RX, int RY, int NS, bool TMA>
 __global__ void __launch_bounds__(TileCfg<T, K, RX, RY, NS>::NT, TileCfg<T, K, RX, RY, NS>::MINB)
 rk4_2d_fused(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items, int n_items,
-             int j_step) {
+             int j_step, int* __restrict__ wait_flag) {
   typedef typename C2<T>::type C;
   typedef TileCfg<T, K, RX, RY, NS> G;
   constexpr int NJ = G::NJ, H = G::H;
@@ -290,7 +292,7 @@ rk4_2d_fused(const Inst2D* __restrict__ insts, const TileItem* __restrict__ item
       if (threadIdx.x == 0) ok = mbar_wait(bar, phase);
       if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) {
-          atomicExch(&g_tile_wait_timeout, 1);
+          atomicExch(wait_flag, 1);  // the launching context's own status word
           mbar_wait(bar, phase);   // let the copy in flight land before the CTA leaves
         }
         return;
@@ -432,7 +434,7 @@ int tile_region_x(int shape) {
     case TILE_64x64W: return 64; case TILE_128x32W: return 128;
     case TILE_64xO64: return 64; case TILE_64xO64M: return 64;
     case TILE_R64x80: case TILE_R64x96: case TILE_R64x96S: case TILE_R64x64: case TILE_R64x72:
-    case TILE_R64x72W: case TILE_R64x80S: return 64;
+    case TILE_R64x72W: case TILE_R64x80S: case TILE_STREAM: return 64;
   }
   return 0;
 }
@@ -454,6 +456,7 @@ int tile_out_x(int shape, int K) { return tile_region_x(shape) - 8 * K; }
 int tile_out_y(int shape, int K) { return tile_region_y(shape, K) - 8 * K; }
 bool tile_supported(int shape, int dtype) {
   if (shape == TILE_32x32) return true;
+  if (shape == TILE_STREAM) return dtype == NLS_C64;
   if (shape == TILE_64x64 || shape == TILE_128x32 || shape == TILE_64x64W || shape == TILE_128x32W ||
       shape == TILE_64xO64 || shape == TILE_64xO64M || reg_shape(shape))
     return dtype == NLS_C64;
@@ -468,10 +471,10 @@ static size_t smem_f() {
 
 template <typename T, int K, int RX, int RY, int NS, bool TMA = false>
 static cudaError_t launch_f(const Inst2D* d_insts, const TileItem* d_items, int n_items, int j_step,
-                            int grid, cudaStream_t s) {
+                            int grid, cudaStream_t s, int* wait_flag = nullptr) {
   typedef TileCfg<T, K, RX, RY, NS> G;
   auto kern = rk4_2d_fused<T, K, RX, RY, NS, TMA>;
-  kern<<<grid, G::NT, smem_f<T, K, RX, RY, NS, TMA>(), s>>>(d_insts, d_items, n_items, j_step);
+  kern<<<grid, G::NT, smem_f<T, K, RX, RY, NS, TMA>(), s>>>(d_insts, d_items, n_items, j_step, wait_flag);
   return cudaGetLastError();
 }
 
@@ -490,8 +493,8 @@ static int occ_f() {
 
 template <typename T, int K, int RX, int RY, int NS>
 static cudaError_t launch_ft(const Inst2D* d_insts, const TileItem* d_items, int n_items, int j_step,
-                             int grid, cudaStream_t s) {
-  return launch_f<T, K, RX, RY, NS, true>(d_insts, d_items, n_items, j_step, grid, s);
+                             int grid, cudaStream_t s, int* wait_flag) {
+  return launch_f<T, K, RX, RY, NS, true>(d_insts, d_items, n_items, j_step, grid, s, wait_flag);
 }
 template <typename T, int K, int RX, int RY, int NS>
 static int occ_ft() {
@@ -500,9 +503,9 @@ static int occ_ft() {
 
 template <int K, int NW, int NJ, bool TMA>
 static cudaError_t launch_r(const Inst2D* d_insts, const TileItem* d_items, int n_items, int j_step,
-                            int grid, cudaStream_t s) {
+                            int grid, cudaStream_t s, int* wait_flag = nullptr) {
   typedef RegCfg<K, NW, NJ> G;
-  rk4_2d_reg<K, NW, NJ, TMA><<<grid, G::NT, G::SMEM, s>>>(d_insts, d_items, n_items, j_step);
+  rk4_2d_reg<K, NW, NJ, TMA><<<grid, G::NT, G::SMEM, s>>>(d_insts, d_items, n_items, j_step, wait_flag);
   return cudaGetLastError();
 }
 // Sets the shared-memory attribute (outside any capture) and returns CTAs per SM.
@@ -593,16 +596,16 @@ int fused_2d_tma_blocks_per_sm(int K, int shape) {
 }
 
 cudaError_t launch_2d_fused_tma(int K, int shape, const Inst2D* d_insts, const TileItem* d_items,
-                                int n_items, int j_step, int grid, cudaStream_t s) {
+                                int n_items, int j_step, int grid, cudaStream_t s, int* wait_flag) {
   if (n_items <= 0) return cudaSuccess;
-  if (!tile_supported(shape, NLS_C64)) return cudaErrorInvalidValue;
+  if (!tile_supported(shape, NLS_C64) || !wait_flag) return cudaErrorInvalidValue;
   if (reg_shape(shape)) {
-    if (K == 1) { NLSG_REG_SHAPES(1, true, launch_r, d_insts, d_items, n_items, j_step, grid, s) }
-    if (K == 2) { NLSG_REG_SHAPES(2, true, launch_r, d_insts, d_items, n_items, j_step, grid, s) }
+    if (K == 1) { NLSG_REG_SHAPES(1, true, launch_r, d_insts, d_items, n_items, j_step, grid, s, wait_flag) }
+    if (K == 2) { NLSG_REG_SHAPES(2, true, launch_r, d_insts, d_items, n_items, j_step, grid, s, wait_flag) }
     return cudaErrorInvalidValue;
   }
-  if (K == 1) { NLSG_SHAPES(float, 1, launch_ft, d_insts, d_items, n_items, j_step, grid, s) }
-  if (K == 2) { NLSG_SHAPES(float, 2, launch_ft, d_insts, d_items, n_items, j_step, grid, s) }
+  if (K == 1) { NLSG_SHAPES(float, 1, launch_ft, d_insts, d_items, n_items, j_step, grid, s, wait_flag) }
+  if (K == 2) { NLSG_SHAPES(float, 2, launch_ft, d_insts, d_items, n_items, j_step, grid, s, wait_flag) }
   return cudaErrorInvalidValue;
 }
 
@@ -653,13 +656,109 @@ cudaError_t tile_tx_extra_set(unsigned bytes) {
   return cudaMemcpyToSymbol(g_tile_tx_extra, &bytes, sizeof(bytes));
 }
 
-int tile_wait_timeout_read_clear(cudaStream_t s) {
-  int v = 0, zero = 0;
-  if (cudaMemcpyFromSymbolAsync(&v, g_tile_wait_timeout, sizeof(int), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess)
-    return -1;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
-  if (v) cudaMemcpyToSymbolAsync(g_tile_wait_timeout, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s);
-  return v;
+// ---- streaming step (complex64): occupancy, launch, work items
+
+template <int K>
+static int occ_s() {
+  typedef StreamCfg<K> G;
+  auto kern = rk4_2d_stream<K>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM) != cudaSuccess)
+    return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, G::NT, G::SMEM) != cudaSuccess) return 0;
+  return nb;
+}
+
+int stream_2d_blocks_per_sm(int K) { return K == 1 ? occ_s<1>() : (K == 2 ? occ_s<2>() : 0); }
+int stream_2d_warps_per_block() { return StreamCfg<1>::WARPS; }
+
+cudaError_t launch_2d_stream(int K, const Inst2D* d_insts, const StripItem* d_items, int n_items, int j_step,
+                             int grid, unsigned* counter, cudaStream_t s) {
+  if (n_items <= 0) return cudaSuccess;
+  if (!counter || grid <= 0) return cudaErrorInvalidValue;
+  if (K == 1) rk4_2d_stream<1><<<grid, StreamCfg<1>::NT, StreamCfg<1>::SMEM, s>>>(d_insts, d_items, n_items, j_step, counter);
+  else if (K == 2) rk4_2d_stream<2><<<grid, StreamCfg<2>::NT, StreamCfg<2>::SMEM, s>>>(d_insts, d_items, n_items, j_step, counter);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+void stream_strips(int n, int K, std::vector<StripGeom>& out) {
+  const int H = 4 * K;
+  out.clear();
+  if (n <= 64) {
+    out.push_back(StripGeom{0, 0, n});
+    return;
+  }
+  // first strip against the left grid edge (no left halo), interior strips with a halo of H on
+  // both sides, last strip against the right grid edge
+  out.push_back(StripGeom{0, 0, 64 - H});
+  int ox = 64 - H;
+  while (ox + 64 - H < n) {
+    out.push_back(StripGeom{ox - H, ox, ox + 64 - 2 * H});
+    ox += 64 - 2 * H;
+  }
+  out.push_back(StripGeom{n - 64, ox, n});
+}
+
+// Row segments of one strip: nseg = ceil(n / ly) pieces of near-equal height.
+static void segments(int n, int ly, std::vector<std::pair<int, int>>& out) {
+  out.clear();
+  const int nseg = std::max(1, (n + ly - 1) / std::max(1, ly));
+  for (int k = 0; k < nseg; ++k) {
+    const int a = (int)((int64_t)k * n / nseg), b = (int)((int64_t)(k + 1) * n / nseg);
+    if (b > a) out.emplace_back(a, b);
+  }
+}
+
+// Estimated makespan (in strip-row iterations) of the items that segment height ly gives over
+// `slots` warps: the mean load per warp plus half the longest item (the expected tail).
+static double stream_cost(const std::vector<int>& ns, int K, int ly, int64_t slots) {
+  std::vector<StripGeom> st;
+  std::vector<std::pair<int, int>> sg;
+  double total = 0.0, longest = 0.0;
+  for (int n : ns) {
+    stream_strips(n, K, st);
+    segments(n, ly, sg);
+    for (auto& g : sg) {
+      // iterations of the wavefront (warm-up and drain rows inside the grid included)
+      const double it = (double)(g.second - g.first) + (g.first > 0 ? 4 * K : 0) + 4 * K;
+      total += it * (double)st.size();
+      longest = std::max(longest, it);
+    }
+  }
+  return total / (double)std::max<int64_t>(1, slots) + 0.5 * longest;
+}
+
+int stream_choose_ly(const std::vector<int>& ns, int K, int64_t slots) {
+  int nmax = 1;
+  for (int n : ns) nmax = std::max(nmax, n);
+  int best = nmax;
+  double best_c = stream_cost(ns, K, nmax, slots);
+  for (int ly = 16; ly < nmax; ly += (ly < 128 ? 8 : (ly < 512 ? 32 : 128))) {
+    const double cst = stream_cost(ns, K, ly, slots);
+    if (cst < best_c * 0.999) {
+      best_c = cst;
+      best = ly;
+    }
+  }
+  return best;
+}
+
+void stream_items(int inst, int n, int K, int ly, std::vector<StripItem>& out) {
+  std::vector<StripGeom> st;
+  std::vector<std::pair<int, int>> sg;
+  stream_strips(n, K, st);
+  segments(n, ly, sg);
+  for (auto& g : st)
+    for (auto& y : sg)
+      out.push_back(StripItem{inst, (uint16_t)g.x0, (uint16_t)g.ox0, (uint16_t)g.ox1, (uint16_t)y.first,
+                              (uint16_t)y.second, 0});
+}
+
+void stream_sort_items(std::vector<StripItem>& items) {
+  std::stable_sort(items.begin(), items.end(), [](const StripItem& a, const StripItem& b) {
+    return (a.y1 - a.y0) > (b.y1 - b.y0);
+  });
 }
 
 cudaError_t launch_2d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,

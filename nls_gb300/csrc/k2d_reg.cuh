@@ -243,7 +243,8 @@ __device__ __forceinline__ void reg_step(float2 (&uX)[NJ], float2 (&uY)[NJ], con
 
 template <int K, int NW, int NJ, bool TMA>
 __global__ void __launch_bounds__(NW * 32, 1)
-rk4_2d_reg(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items, int n_items, int j_step) {
+rk4_2d_reg(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items, int n_items, int j_step,
+           int* __restrict__ wait_flag) {
   typedef RegCfg<K, NW, NJ> G;
   constexpr int H = G::H;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -385,7 +386,7 @@ rk4_2d_reg(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items,
     if (threadIdx.x == 0) ok = mbar_wait(bar, phase);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
-        atomicExch(&g_tile_wait_timeout, 1);
+        atomicExch(wait_flag, 1);  // the launching context's own status word
         mbar_wait(bar, phase);  // let the copies in flight land before the CTA leaves
       }
       return;

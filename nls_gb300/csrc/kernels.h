@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "nls_types.h"
 
 // dtype codes shared with the public C ABI
@@ -44,6 +46,9 @@ enum TileShape2D {
   TILE_R64x72 = 12,   // 8 warps x 9 rows (256 threads): 64 output rows at order 3
   TILE_R64x72W = 13,  // 12 warps x 6 rows (384 threads)
   TILE_R64x80S = 14,  // 8 warps x 10 rows (256 threads): 64 output rows at order 5
+  // streaming wavefront (rk4_2d_stream, single precision): warp = 64-column strip walking down
+  // a segment of rows, work items taken from a launch-wide counter
+  TILE_STREAM = 15,
 };
 int tile_region_x(int shape);
 int tile_region_y(int shape, int K);
@@ -56,18 +61,36 @@ cudaError_t launch_2d_fused(int dtype, int K, int shape, const Inst2D* d_insts,
                             const TileItem* d_items, int n_items, int j_step, int grid,
                             cudaStream_t s);
 // TMA path of the fused step (complex64 only): one elected thread per CTA prefetches the next
-// tile's state and pump boxes with cp.async.bulk.tensor while the current tile is computed.
+// tile's state and pump boxes with cp.async.bulk.tensor while the current tile is computed.  A
+// bounded wait on those copies that expires sets *wait_flag (the launching context's status word,
+// a device int) and the CTA leaves.
 bool tma_eligible(int dtype, int n, const void* u0, const void* u1, const void* P);
 size_t tma_map_bytes();  // bytes of the 3 tensor maps of one instance (128-byte aligned slot)
 int tma_encode_2d(int shape, int K, int n, const void* u0, const void* u1, const void* P, void* out_maps);
 int fused_2d_tma_blocks_per_sm(int K, int shape);
 cudaError_t launch_2d_fused_tma(int K, int shape, const Inst2D* d_insts, const TileItem* d_items,
-                                int n_items, int j_step, int grid, cudaStream_t s);
-// 1 if a bounded tile wait expired since the last call (then cleared), 0 if not, -1 on error
-int tile_wait_timeout_read_clear(cudaStream_t s);
+                                int n_items, int j_step, int grid, cudaStream_t s, int* wait_flag);
 // Test control: arm every tile barrier of the register-tile kernel for this many bytes more than
 // its copies deliver (0 = normal operation), on the current device.
 cudaError_t tile_tx_extra_set(unsigned bytes);
+// Streaming step (TILE_STREAM): CTAs per SM (sets the shared-memory attribute; call outside any
+// capture), warps per CTA, and the launch.  counter: two device unsigned ints, zero before the
+// first launch; every launch leaves them zero again.
+int stream_2d_blocks_per_sm(int K);
+int stream_2d_warps_per_block();
+cudaError_t launch_2d_stream(int K, const Inst2D* d_insts, const StripItem* d_items, int n_items, int j_step,
+                             int grid, unsigned* counter, cudaStream_t s);
+// Strip geometry of an n-wide grid (first strip against the left edge, interior strips with a
+// 4K halo on both sides, last strip against the right edge), the segment height that minimises
+// the estimated makespan of a set of grids over `slots` warps, the items of one instance, and
+// the longest-first order the kernel takes them in.
+struct StripGeom {
+  int x0, ox0, ox1;
+};
+void stream_strips(int n, int K, std::vector<StripGeom>& out);
+int stream_choose_ly(const std::vector<int>& ns, int K, int64_t slots);
+void stream_items(int inst, int n, int K, int ly, std::vector<StripItem>& out);
+void stream_sort_items(std::vector<StripItem>& items);
 cudaError_t launch_2d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,
                             void* acc, void* dst, double dt, const PhysD& ph, const Stencil2D& op,
                             cudaStream_t st);

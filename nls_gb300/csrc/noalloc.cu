@@ -10,9 +10,10 @@
 // rk4_2d_fused tile, since the stage kernels nls_solve_device uses there need more scratch), but
 // its scratch -- the second state buffer of the ping-pong, the instance descriptor and the tile
 // list -- lives in one file-scope __device__ array of fixed size, so the call allocates nothing.
+#include <cuda.h>
+
 #include <cstring>
 #include <mutex>
-#include <vector>
 
 #include "../../include/nls_gb300.h"
 #include "kernels.h"
@@ -39,22 +40,67 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 static_assert(sizeof(Inst2D) <= kDescBytes, "descriptor slot too small");
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_dev[kMaxDevices] = {nullptr};
+// Writes the call's descriptor (passed by value as a kernel parameter) and its tile list
+// {0, t} into the scratch array, so that no host memory is read after the call returns.
+__global__ void noalloc_setup(Inst2D I, Inst2D* __restrict__ dI, TileItem* __restrict__ items, int n_items) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) *dI = I;
+  if (t < n_items) items[t] = TileItem{0, t};
+}
 
-// Device address of the scratch array on the current device; resolved once per device.
-cudaError_t scratch_address(int device, char** out) {
-  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_dev[device]) {
+// The symbol address is resolved per CUDA context (the array is a module global, instantiated
+// once in every context that loads the module), keyed by the current driver context.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+
+CtxGetCurrentFn ctx_get_current() {
+  static std::once_flag once;
+  static CtxGetCurrentFn fn = nullptr;
+  std::call_once(once, [] {
     void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    if (!p) return cudaErrorInvalidSymbol;
-    g_scratch_dev[device] = p;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(p);
+  });
+  return fn;
+}
+
+constexpr int kMaxContexts = 64;
+std::mutex g_mu;
+CUcontext g_ctx[kMaxContexts] = {};
+void* g_addr[kMaxContexts] = {};
+
+// Device address of the scratch array in the current context: resolved with cudaGetSymbolAddress
+// the first time a context calls in (which also binds the device's primary context when no
+// context is current), then taken from the cache.
+cudaError_t scratch_address(char** out) {
+  CtxGetCurrentFn get = ctx_get_current();
+  if (!get) return cudaErrorNotSupported;
+  CUcontext cur = nullptr;
+  if (get(&cur) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto find = [&](CUcontext c) -> int {
+    for (int i = 0; i < kMaxContexts; ++i)
+      if (c && g_ctx[i] == c) return i;
+    return -1;
+  };
+  int slot = find(cur);
+  if (slot >= 0) {
+    *out = (char*)g_addr[slot];
+    return cudaSuccess;
   }
-  *out = (char*)g_scratch_dev[device];
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  if (!p) return cudaErrorInvalidSymbol;
+  if (!cur && (get(&cur) != CUDA_SUCCESS || !cur)) return cudaErrorDeviceUninitialized;
+  slot = find(cur);
+  for (int i = 0; i < kMaxContexts && slot < 0; ++i)
+    if (!g_ctx[i]) slot = i;
+  if (slot < 0) slot = (int)(reinterpret_cast<uintptr_t>(cur) % kMaxContexts);  // table full: replace one
+  g_ctx[slot] = cur;
+  g_addr[slot] = p;
+  *out = (char*)p;
   return cudaSuccess;
 }
 
@@ -70,10 +116,14 @@ NLS_API int nls_solve_2d_noalloc(int dtype, const nls_problem* pr, int64_t iters
   if ((int64_t)pr->n * pr->n > (int64_t)NLS_NOALLOC_MAX_NODES) return NLS_ERR_TOO_LARGE;
   Stencil2D op;
   if (host_stencil_2d(pr->order, pr->dx, &op)) return NLS_ERR_ORDER;
-  // fused tile shape: the caller's choice if it names a fused tile this precision supports,
-  // otherwise the register-resident 64x96 tile (complex64) or the 32x32 tile (complex128)
+  // fused tile shape: -1 = the register-resident 64x96 tile (complex64) or the 32x32 tile
+  // (complex128); otherwise a fused tile this precision supports (0, the unfused stage kernels,
+  // needs three more state-sized buffers and is not offered here)
   int shape = dtype == NLS_C64 ? TILE_R64x96S : TILE_32x32;
-  if (pr->variant > 0 && tile_supported(pr->variant, dtype)) shape = pr->variant;
+  if (pr->variant >= 0) {
+    if (pr->variant == 0 || !tile_supported(pr->variant, dtype)) return NLS_ERR_INVALID;
+    shape = pr->variant;
+  }
   const int n = pr->n;
   const int tx = tile_out_x(shape, op.K), ty = tile_out_y(shape, op.K);
   const int tiles_x = (n + tx - 1) / tx;
@@ -84,7 +134,7 @@ NLS_API int nls_solve_2d_noalloc(int dtype, const nls_problem* pr, int64_t iters
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess) return NLS_ERR_CUDA;
   char* base = nullptr;
-  if (scratch_address(device, &base) != cudaSuccess) return NLS_ERR_CUDA;
+  if (scratch_address(&base) != cudaSuccess) return NLS_ERR_CUDA;
   void* state2 = base;
   Inst2D* dI = (Inst2D*)(base + kStateBytes);
   TileItem* dT = (TileItem*)(base + kStateBytes + kDescBytes);
@@ -104,17 +154,14 @@ NLS_API int nls_solve_2d_noalloc(int dtype, const nls_problem* pr, int64_t iters
   I.ph.c12 = pr->coeffs[11]; I.ph.c13 = pr->coeffs[12]; I.ph.c14 = pr->coeffs[13];
   I.op = op;
   set_params(I);
-  std::vector<TileItem> items(n_items);
-  for (int t = 0; t < n_items; ++t) items[t] = TileItem{0, t};
-  // Pageable host sources: each copy returns once its bytes are staged, so the host vectors
-  // may go out of scope afterwards; the kernels below are ordered after the copies on `st`.
-  if (cudaMemcpyAsync(dI, &I, sizeof(I), cudaMemcpyHostToDevice, st) != cudaSuccess) return NLS_ERR_CUDA;
-  if (cudaMemcpyAsync(dT, items.data(), sizeof(TileItem) * n_items, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return NLS_ERR_CUDA;
+  noalloc_setup<<<(n_items + 255) / 256, 256, 0, st>>>(I, dI, dT, n_items);
+  if (cudaGetLastError() != cudaSuccess) return NLS_ERR_CUDA;
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return NLS_ERR_CUDA;
   const int occ = fused_2d_blocks_per_sm(dtype, op.K, shape);
   const int grid = n_items < sms * (occ > 0 ? occ : 1) ? n_items : sms * (occ > 0 ? occ : 1);
+  // The non-TMA form of the tile kernels: every thread loads its own nodes, so no launch of this
+  // call waits on a copy barrier and none can time out.
   for (int64_t j = 0; j < iters; ++j) {
     if (launch_2d_fused(dtype, op.K, shape, dI, dT, n_items, (int)(j & 1), grid, st) != cudaSuccess)
       return NLS_ERR_CUDA;

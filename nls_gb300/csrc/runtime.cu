@@ -68,6 +68,10 @@ struct nls_ctx {
   DevBuf diag;      // diagnostics partials and results
   DevBuf diagv;     // H(u) scratch of the device chemical potential
   double* h_diag = nullptr;  // pinned
+  // Status word of the bounded tile waits of this context's launches (a device int set by a
+  // fused 2-D kernel whose copy wait expired), and its pinned host mirror.
+  int* wait_flag = nullptr;
+  int* h_wait_flag = nullptr;
 };
 
 static int fail(nls_ctx* ctx, int code, const std::string& msg) {
@@ -90,11 +94,18 @@ static int fail_cuda(nls_ctx* ctx, cudaError_t e, const char* what) {
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// A bounded wait inside a tile kernel that expired leaves a device flag; report it once.
+// A bounded wait inside one of this context's tile kernels that expired leaves the context's
+// status word set; report it once (then clear it).  Synchronises the context's stream.
 static int check_timeout(nls_ctx* ctx) {
-  const int t = tile_wait_timeout_read_clear(ctx->stream);
-  if (t < 0) return fail(ctx, NLS_ERR_CUDA, "reading the tile-wait flag failed");
-  if (t > 0) return fail(ctx, NLS_ERR_TIMEOUT, "a tile copy did not arrive within its bounded wait");
+  if (cudaMemcpyAsync(ctx->h_wait_flag, ctx->wait_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+    return fail(ctx, NLS_ERR_CUDA, "reading the tile-wait status word failed");
+  if (*ctx->h_wait_flag) {
+    *ctx->h_wait_flag = 0;
+    cudaMemsetAsync(ctx->wait_flag, 0, sizeof(int), ctx->stream);
+    return fail(ctx, NLS_ERR_TIMEOUT, "a tile copy did not arrive within its bounded wait");
+  }
   return NLS_OK;
 }
 static size_t csize(int dtype) { return dtype == NLS_C128 ? 16 : 8; }
@@ -296,7 +307,7 @@ static int solve_2d_dev(nls_ctx* ctx, int dtype, const nls_problem* pr, int64_t 
   const int occ = tma ? fused_2d_tma_blocks_per_sm(op.K, shape) : fused_2d_blocks_per_sm(dtype, op.K, shape);
   const int grid = std::max(1, std::min(n_items, ctx->sm_count * std::max(1, occ)));
   auto launch = [&](int j) -> cudaError_t {
-    return tma ? launch_2d_fused_tma(op.K, shape, dI, dT, n_items, j, grid, ctx->stream)
+    return tma ? launch_2d_fused_tma(op.K, shape, dI, dT, n_items, j, grid, ctx->stream, ctx->wait_flag)
                : launch_2d_fused(dtype, op.K, shape, dI, dT, n_items, j, grid, ctx->stream);
   };
   const int S = 64;  // even: a replay returns the state to the caller's buffer
@@ -706,7 +717,8 @@ static cudaError_t batch_sequence(nls_batch* b, int64_t steps) {
   }
   for (int64_t j = 0; j < steps; ++j) {
     for (auto& G : b->g2)
-      if ((e = G.tma ? launch_2d_fused_tma(G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream)
+      if ((e = G.tma ? launch_2d_fused_tma(G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream,
+                                           ctx->wait_flag)
                      : launch_2d_fused(dtype, G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream)))
         return e;
     for (auto& M : b->m) {
@@ -816,6 +828,8 @@ static void ctx_release(nls_ctx* ctx) {
   ctx->diag.release();
   ctx->diagv.release();
   if (ctx->h_diag) cudaFreeHost(ctx->h_diag);
+  if (ctx->wait_flag) cudaFree(ctx->wait_flag);
+  if (ctx->h_wait_flag) cudaFreeHost(ctx->h_wait_flag);
   for (int i = 0; i < nls_ctx::kSide; ++i) {
     if (ctx->side_done[i]) cudaEventDestroy(ctx->side_done[i]);
     if (ctx->side[i]) cudaStreamDestroy(ctx->side[i]);
@@ -845,6 +859,10 @@ NLS_API int nls_ctx_create(int device, nls_ctx** out) {
   for (int i = 0; ok && i < nls_ctx::kSide; ++i)
     ok = cudaStreamCreateWithFlags(&ctx->side[i], cudaStreamNonBlocking) == cudaSuccess &&
          cudaEventCreateWithFlags(&ctx->side_done[i], cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaMalloc(&ctx->wait_flag, sizeof(int)) == cudaSuccess &&
+       cudaMallocHost(&ctx->h_wait_flag, sizeof(int)) == cudaSuccess &&
+       cudaMemset(ctx->wait_flag, 0, sizeof(int)) == cudaSuccess;
+  if (ok) *ctx->h_wait_flag = 0;
   if (!ok) {
     ctx_release(ctx);
     return NLS_ERR_CUDA;
@@ -1383,7 +1401,8 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
     for (auto& L : l2) {
       const Inst2D* dI = (const Inst2D*)(d + L.off);
       const TileItem* dT = (const TileItem*)(d + L.off_items);
-      CK(ctx, L.tma ? launch_2d_fused_tma(L.K, L.shape, dI, dT, L.n_items, (int)j, L.grid, ctx->stream)
+      CK(ctx, L.tma ? launch_2d_fused_tma(L.K, L.shape, dI, dT, L.n_items, (int)j, L.grid, ctx->stream,
+                                          ctx->wait_flag)
                     : launch_2d_fused(dtype, L.K, L.shape, dI, dT, L.n_items, (int)j, L.grid, ctx->stream));
       ctx->launches += 1;
     }

@@ -226,3 +226,26 @@ def test_autotune_batch_refines_1d_cluster_sizes_on_the_batch(monkeypatch):
     single = [w.mix_instance(i, 1, with_data=False) for i in range(5)]
     autotune.apply(single, dtype=np.complex64, mode="single")
     assert all(s.variant == 16 for s in single)
+
+
+def test_native_alias_binds_the_gpu_module_object():
+    """The documented drop-in alias: with ``sys.modules["nls.native"]`` set to ``nls_gb300.native``,
+    the reference's ``from .native import nls`` (nls/solver.py:9) binds the GPU module object."""
+    import sys
+    import types
+    import nls_gb300.native
+    saved = {k: sys.modules.get(k) for k in ("nls", "nls.native")}
+    try:
+        pkg = types.ModuleType("nls")
+        pkg.__path__ = []
+        sys.modules["nls"] = pkg
+        sys.modules["nls.native"] = nls_gb300.native
+        from nls.native import nls as bound  # noqa: E402
+        assert bound is nls_gb300.native.nls
+        assert callable(bound.solve_nls) and callable(bound.solve_nls_2d)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v

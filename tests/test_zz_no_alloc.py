@@ -1,14 +1,18 @@
-"""The allocation-free 2-D entry point (nls_solve_2d_noalloc) against nls_solve_device.
+"""The allocation-free 2-D entry point (nls_solve_2d_noalloc) against nls_solve_device and the oracle.
 
 Some callers of this library may not allocate device memory at all -- a service that reserves its
 device budget once at start-up, a framework whose caching allocator owns the GPU memory, or a
 latency-critical loop that cannot afford cudaMalloc's possible device-wide synchronisation.  For
 them the library exposes one 2-D solve whose scratch is a fixed device array inside the library.
 This test calls it through the C ABI twice in a row (different sizes and orders, so the second
-call runs over whatever the first left in the shared array) and checks each result against the
-ordinary entry point running the same kernel, within the parity tolerances of the other GPU
-tests (1e-10 relative L2 for complex128, 3e-5 for complex64).  It is collected last so that a
-failure here never hides the rest of the suite, and it runs the same alone or after the others.
+call runs over whatever the first left in the shared array) and checks each result bit for bit
+against the ordinary entry point running the same tile kernel, and against the oracle at the
+suite's parity tolerances (1e-10 relative L2 for complex128 vs the FP64 oracle; 3e-5 for
+complex64 vs the FP32 oracle).  It also checks that the device's free memory does not change
+across calls, that the kernel form it runs has no copy barrier (arming the test control that
+makes those barriers expire changes nothing), and that invalid variants are refused.  It is
+collected last so that a failure here never hides the rest of the suite, and it runs the same
+alone or after the others.
 """
 
 import ctypes
@@ -39,39 +43,78 @@ def _case(n, order, seed):
     return s
 
 
-@pytest.mark.parametrize("dtype,variant,tol", [(np.complex64, 1, 3e-5), (np.complex64, 10, 3e-5),
-                                               (np.complex128, 3, 1e-10)])
-def test_noalloc_matches_solve_device_on_two_calls(env, dtype, variant, tol):
+def _noalloc(torch, _lib, code, s, n, order, iters, P, u, variant):
+    pr = _lib.make_problem(2, n, order, s.dt, s.dx, s.coeffs, variant)
+    stream = torch.cuda.current_stream()
+    return _lib.lib().nls_solve_2d_noalloc(code, ctypes.byref(pr), iters, ctypes.c_void_p(P.data_ptr()),
+                                           ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+
+
+@pytest.mark.parametrize("dtype,variant", [(np.complex64, -1), (np.complex64, 1), (np.complex64, 10),
+                                           (np.complex64, 12), (np.complex128, 3), (np.complex128, -1)])
+def test_noalloc_matches_solve_device_on_two_calls(env, oracle_lib, dtype, variant):
     torch, _lib = env
     from nls_gb300 import device
-    lib = _lib.lib()
     code = _lib.dtype_code(dtype)
     ct = torch.complex64 if dtype == np.complex64 else torch.complex128
     rt = torch.float32 if dtype == np.complex64 else torch.float64
+    same = variant if variant > 0 else (10 if dtype == np.complex64 else 3)   # the default tile
+    # 130: rows not 16-byte multiples; 96: a multiple of 4 (nls_solve_device takes its TMA form)
     for call, (n, order, iters, seed) in enumerate([(130, 5, 41, 1), (96, 3, 40, 2)]):
         s = _case(n, order, seed)
-        P = torch.tensor(np.ascontiguousarray(s.pumping), dtype=rt, device="cuda")
-        u_ref = torch.tensor(np.ascontiguousarray(s.u0), dtype=ct, device="cuda")
+        # torch row-major (n, n) with the last index contiguous == the Fortran-order memory
+        P = torch.tensor(np.ascontiguousarray(s.pumping.T), dtype=rt, device="cuda")
+        u_ref = torch.tensor(np.ascontiguousarray(s.u0.T), dtype=ct, device="cuda")
         u_new = u_ref.clone()
-        device.solve_(u_ref, P, order=order, dt=s.dt, dx=s.dx, coeffs=s.coeffs, iters=iters, variant=variant)
-        pr = _lib.make_problem(2, n, order, s.dt, s.dx, s.coeffs, variant)
-        stream = torch.cuda.current_stream()
-        st = lib.nls_solve_2d_noalloc(code, ctypes.byref(pr), iters, ctypes.c_void_p(P.data_ptr()),
-                                      ctypes.c_void_p(u_new.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        device.solve_(u_ref, P, order=order, dt=s.dt, dx=s.dx, coeffs=s.coeffs, iters=iters, variant=same)
+        st = _noalloc(torch, _lib, code, s, n, order, iters, P, u_new, variant)
         assert st == _lib.NLS_OK, (call, st)
         torch.cuda.synchronize()
         a, b = u_new.cpu().numpy(), u_ref.cpu().numpy()
         assert np.all(np.isfinite(a))
-        assert rel(a, b) <= tol, (call, rel(a, b))
+        assert np.array_equal(a, b), (call, rel(a, b))
+        want = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0,
+                                dtype=np.float64 if dtype == np.complex128 else np.float32)
+        assert rel(a.T, want) <= (1e-10 if dtype == np.complex128 else 3e-5), call
 
 
-def test_noalloc_rejects_grids_beyond_its_limit(env):
+def test_noalloc_allocates_no_device_memory_and_has_no_copy_barrier(env):
+    torch, _lib = env
+    s = _case(152, 3, 4)
+    P = torch.tensor(np.ascontiguousarray(s.pumping.T), dtype=torch.float32, device="cuda")
+    u0 = torch.tensor(np.ascontiguousarray(s.u0.T), dtype=torch.complex64, device="cuda")
+    u = u0.clone()
+    for v in (10, 12, -1):      # warm-up: every kernel the measured calls launch is loaded once
+        assert _noalloc(torch, _lib, _lib.NLS_C64, s, 152, 3, 3, P, u, v) == _lib.NLS_OK
+    torch.cuda.synchronize()
+    outs = [u0.clone() for _ in range(3)]
+    free0 = torch.cuda.mem_get_info()[0]
+    assert _lib.lib().nls_test_set_tile_tx_extra(0, 16) == _lib.NLS_OK
+    try:
+        for v, out in zip((10, 12, -1), outs):
+            assert _noalloc(torch, _lib, _lib.NLS_C64, s, 152, 3, 25, P, out, v) == _lib.NLS_OK
+        torch.cuda.synchronize()
+    finally:
+        assert _lib.lib().nls_test_set_tile_tx_extra(0, 0) == _lib.NLS_OK
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0
+    from nls_gb300 import device
+    ref = u0.clone()
+    device.solve_(ref, P, order=3, dt=s.dt, dx=s.dx, coeffs=s.coeffs, iters=25, variant=10)
+    torch.cuda.synchronize()
+    assert torch.equal(outs[0], ref) and torch.equal(outs[2], ref)
+
+
+def test_noalloc_rejects_bad_variants_and_grids_beyond_its_limit(env):
     torch, _lib = env
     lib = _lib.lib()
-    n = 513                                    # 513 * 513 > NLS_NOALLOC_MAX_NODES
     s = _case(16, 3, 0)
+    dummy = torch.zeros(16 * 16, dtype=torch.complex64, device="cuda")
+    P = torch.zeros(16 * 16, dtype=torch.float32, device="cuda")
+    n = 513                                    # 513 * 513 > NLS_NOALLOC_MAX_NODES
     pr = _lib.make_problem(2, n, 3, s.dt, s.dx, s.coeffs, -1)
-    dummy = torch.zeros(4, dtype=torch.complex64, device="cuda")
-    st = lib.nls_solve_2d_noalloc(_lib.NLS_C64, ctypes.byref(pr), 1, ctypes.c_void_p(dummy.data_ptr()),
+    st = lib.nls_solve_2d_noalloc(_lib.NLS_C64, ctypes.byref(pr), 1, ctypes.c_void_p(P.data_ptr()),
                                   ctypes.c_void_p(dummy.data_ptr()), None)
     assert st == _lib.NLS_ERR_TOO_LARGE
+    for code, v in ((_lib.NLS_C64, 0), (_lib.NLS_C128, 10), (_lib.NLS_C64, 99)):
+        assert _noalloc(torch, _lib, code, s, 16, 3, 1, P, dummy, v) == _lib.NLS_ERR_INVALID
