@@ -1,0 +1,341 @@
+// k2d_stream.cuh -- streaming (wavefront) fused RK4 step over 2-D strips (complex64, sm_103a).
+//
+// Same contract as the tile kernels (one launch = one complete RK4 step of every listed piece of
+// every listed instance, nls/nls.f90:892-900, one HBM pass per step), organised for a warp that
+// never waits for another warp:
+//   * a work item is a vertical strip of 64 columns and a segment of rows [y0, y1) of one
+//     instance; lane l holds the node pair (x0 + 2l, x0 + 2l + 1), planar (X = real parts of both
+//     nodes, Y = imaginary parts) so the right-hand side runs on the packed FP32x2 pipe;
+//   * the warp walks down the rows.  At row i it loads row i (state and pump) and evaluates the
+//     four RK4 stages as a wavefront: stage 1 at row i-K, stage 2 at row i-2K, stage 3 at row i-3K
+//     and stage 4 (the update) at row i-4K, each from the window of its input rows held in
+//     registers (window of W = 4K+1 rows, indexed by row modulo W; the loop is unrolled by W so
+//     every index is a compile-time constant).  Rows are read and written exactly once per step;
+//     the only recomputation is the 4K columns of horizontal halo at strip edges inside the grid
+//     and the 4K rows of warm-up and drain at segment ends inside the grid;
+//   * horizontal neighbours come from the adjacent lanes by warp shuffle; at a strip edge that is
+//     the grid edge the missing neighbours are masked to zero (the reference's truncated
+//     operator), and columns beyond the grid hold zero state with a zero stencil weight, so their
+//     stage values stay exactly zero;
+//   * rows are prefetched D rows ahead with cp.async into a per-warp shared-memory ring (each lane
+//     copies and later reads only its own bytes, so no warp synchronisation is involved; rows
+//     outside the grid arrive zero-filled through the copy's source size);
+//   * warps take items from a launch-wide atomic counter (items are listed longest first), so
+//     uneven items balance across the GPU; the last warp of the launch resets the counter for the
+//     next launch.  No thread ever waits on another thread.
+#pragma once
+
+#include <type_traits>
+
+namespace nlsg {
+
+// Calls f(std::integral_constant<int, P>) for P = B .. E-1 (compile-time unrolling).
+template <int B, int E>
+struct StaticFor {
+  template <typename F>
+  __device__ __forceinline__ static void run(F&& f) {
+    f(std::integral_constant<int, B>{});
+    StaticFor<B + 1, E>::run(f);
+  }
+};
+template <int E>
+struct StaticFor<E, E> {
+  template <typename F>
+  __device__ __forceinline__ static void run(F&&) {}
+};
+
+template <int K>
+struct StreamCfg {
+  static constexpr int H = 4 * K;          // horizontal halo of a strip edge inside the grid
+  static constexpr int W = 4 * K + 1;      // rows held per window (rows i-4K .. i)
+  static constexpr int D = 4;              // rows prefetched ahead of the one being consumed
+  static constexpr int R = 8;              // ring slots per warp (R >= D + 2, a power of two)
+  static constexpr int ROWB = 64 * 8 + 64 * 4;   // one row of a strip: 64 complex64 + 64 float32
+  static constexpr int WARPS = 4;
+  static constexpr int NT = 32 * WARPS;
+  static constexpr size_t SMEM = (size_t)WARPS * R * ROWB;
+  static_assert(R >= D + 2 && (R & (R - 1)) == 0, "ring");
+};
+
+// Per-warp constants of an item: broadcast pairs of the step coefficients (pre-multiplied by
+// dt/2 like the register tile's, see RegConst) and per-lane stencil weights and edge masks.
+struct StreamConst {
+  float2 w1, nw1, w2, nw2;     // +-dt/2 w_d, zero for columns outside the grid
+  float2 nwc, c3, nc4, c5, c6, c13, c14, c12, two, third;
+  float mL, mR;                // 0 where the left / right neighbour lies beyond the grid edge
+  float2 mL2, mR2;
+};
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async_sz(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(dst),
+               "l"(reinterpret_cast<uint64_t>(src)), "n"(BYTES), "r"(src_bytes) : "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Slope of one stage at the centre row of the window (slot C), pre-multiplied by dt/2:
+//   q = a u - i (b - wc) u + i L'u,  L'u = w1 s1 + w2 s2,  a = c3 r - c4,  b = c5 |u|^2 + c6 r,
+//   r = c12 P / (c13 + c14 |u|^2)                                     (nls/nls.f90:570-650)
+template <int K, int W, int C>
+__device__ __forceinline__ void stream_slope(const float2 (&inX)[W], const float2 (&inY)[W], float2 pcv,
+                                             const StreamConst& c, float2& qX, float2& qY) {
+  constexpr int U1 = (C - 1 + W) % W, D1 = (C + 1) % W;
+  const float2 X = inX[C], Y = inY[C];
+  float2 mX, nmY;
+  if (K == 1) {
+    const float lx = __shfl_up_sync(0xffffffffu, X.y, 1), ly = __shfl_up_sync(0xffffffffu, Y.y, 1);
+    const float rx = __shfl_down_sync(0xffffffffu, X.x, 1), ry = __shfl_down_sync(0xffffffffu, Y.x, 1);
+    const float2 sX = add2(add2(f2(__fmaf_rn(c.mL, lx, X.y), __fmaf_rn(c.mR, rx, X.x)), inX[U1]), inX[D1]);
+    const float2 sY = add2(add2(f2(__fmaf_rn(c.mL, ly, Y.y), __fmaf_rn(c.mR, ry, Y.x)), inY[U1]), inY[D1]);
+    mX = mul2(c.w1, sX);
+    nmY = mul2(c.nw1, sY);
+  } else {
+    constexpr int U2 = (C - 2 + 2 * W) % W, D2 = (C + 2) % W;
+    const float2 LX = f2(__shfl_up_sync(0xffffffffu, X.x, 1), __shfl_up_sync(0xffffffffu, X.y, 1));
+    const float2 LY = f2(__shfl_up_sync(0xffffffffu, Y.x, 1), __shfl_up_sync(0xffffffffu, Y.y, 1));
+    const float2 RX = f2(__shfl_down_sync(0xffffffffu, X.x, 1), __shfl_down_sync(0xffffffffu, X.y, 1));
+    const float2 RY = f2(__shfl_down_sync(0xffffffffu, Y.x, 1), __shfl_down_sync(0xffffffffu, Y.y, 1));
+    const float2 s1X = add2(add2(f2(__fmaf_rn(c.mL, LX.y, X.y), __fmaf_rn(c.mR, RX.x, X.x)), inX[U1]), inX[D1]);
+    const float2 s1Y = add2(add2(f2(__fmaf_rn(c.mL, LY.y, Y.y), __fmaf_rn(c.mR, RY.x, Y.x)), inY[U1]), inY[D1]);
+    const float2 s2X = add2(add2(fma2(c.mL2, LX, mul2(c.mR2, RX)), inX[U2]), inX[D2]);
+    const float2 s2Y = add2(add2(fma2(c.mL2, LY, mul2(c.mR2, RY)), inY[U2]), inY[D2]);
+    mX = fma2(c.w2, s2X, mul2(c.w1, s1X));
+    nmY = fma2(c.nw2, s2Y, mul2(c.nw1, s1Y));
+  }
+  const float2 sq = f2(__fmaf_rn(X.x, X.x, Y.x * Y.x), __fmaf_rn(X.y, X.y, Y.y * Y.y));
+  const float2 den = fma2(c.c14, sq, c.c13);
+  const float2 r = mul2(pcv, f2(rcp_approx(den.x), rcp_approx(den.y)));
+  const float2 a = fma2(c.c3, r, c.nc4);
+  const float2 bw = fma2(c.c5, sq, fma2(c.c6, r, c.nwc));
+  qX = fma2(a, X, fma2(bw, Y, nmY));
+  qY = fma2(a, Y, fma2(neg2(bw), X, mX));
+}
+
+// The rolling windows of one warp (registers): state, c12 * pump, RK4 accumulator and the inputs
+// of stages 2, 3 and 4, each by row modulo W.
+template <int W>
+struct StreamWin {
+  float2 uX[W], uY[W], pc[W], aX[W], aY[W];
+  float2 t2X[W], t2Y[W], t3X[W], t3Y[W], t4X[W], t4Y[W];
+};
+
+template <int K>
+__global__ void __launch_bounds__(StreamCfg<K>::NT, K == 1 ? 3 : 2)
+rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ items, int n_items, int j_step,
+              unsigned* __restrict__ counter) {
+  typedef StreamCfg<K> G;
+  constexpr int W = G::W, D = G::D, R = G::R;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t ring = smem_u32(smem_raw + (size_t)warp * R * G::ROWB);
+  const unsigned char* ring_g = smem_raw + (size_t)warp * R * G::ROWB;
+
+  auto fetch = [&]() -> int {
+    unsigned v = 0;
+    if (lane == 0) v = atomicAdd(&counter[0], 1u);
+    return (int)__shfl_sync(0xffffffffu, v, 0);
+  };
+
+  for (int idx = fetch(); idx < n_items; idx = fetch()) {
+    const StripItem it = items[idx];
+    const Inst2D& I = insts[it.inst];
+    if ((int64_t)j_step >= I.steps) continue;
+    const int n = I.n;
+    const int par = (I.parity + j_step) & 1;
+    const float2* __restrict__ src = reinterpret_cast<const float2*>(I.u[par]);
+    float2* __restrict__ dst = reinterpret_cast<float2*>(I.u[par ^ 1]);
+    const float* __restrict__ Pg = reinterpret_cast<const float*>(I.P);
+    const bool even = !(n & 1) &&
+                      ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst) |
+                        reinterpret_cast<uintptr_t>(Pg)) & 15) == 0;
+    const int x = (int)it.x0 + 2 * lane;
+    const bool in0 = x < n, in1 = x + 1 < n;
+    const bool out0 = in0 && x >= (int)it.ox0 && x < (int)it.ox1;
+    const bool out1 = in1 && x + 1 >= (int)it.ox0 && x + 1 < (int)it.ox1;
+    const int y0 = it.y0, y1 = it.y1;
+
+    StreamConst c;
+    {
+      const Params<float>& p = I.pf;
+      const float h = p.half_dt;
+      const float w1 = h * p.w1, w2 = h * p.w2;
+      c.w1 = f2(in0 ? w1 : 0.f, in1 ? w1 : 0.f);
+      c.nw1 = f2(in0 ? -w1 : 0.f, in1 ? -w1 : 0.f);
+      c.w2 = f2(in0 ? w2 : 0.f, in1 ? w2 : 0.f);
+      c.nw2 = f2(in0 ? -w2 : 0.f, in1 ? -w2 : 0.f);
+      c.nwc = f2(-(h * p.wc), -(h * p.wc));
+      c.c3 = f2(h * p.c3, h * p.c3);
+      c.nc4 = f2(-(h * p.c4), -(h * p.c4));
+      c.c5 = f2(h * p.c5, h * p.c5);
+      c.c6 = f2(h * p.c6, h * p.c6);
+      c.c13 = f2(p.c13, p.c13);
+      c.c14 = f2(p.c14, p.c14);
+      c.c12 = f2(p.c12, p.c12);
+      c.two = f2(2.f, 2.f);
+      c.third = f2(1.f / 3.f, 1.f / 3.f);
+      c.mL = (lane == 0 && it.x0 == 0) ? 0.f : 1.f;
+      c.mR = (lane == 31 && (int)it.x0 + 64 == n) ? 0.f : 1.f;
+      c.mL2 = f2(c.mL, c.mL);
+      c.mR2 = f2(c.mR, c.mR);
+    }
+
+    const int ib = y0 - 4 * K > 0 ? y0 - 4 * K : 0;   // first row loaded
+    const int ie = y1 + 4 * K;                        // one past the last iteration
+    // iterations whose load row and four stage rows all lie inside the grid and inside the rows
+    // this segment needs: no per-stage checks
+    const int clean_lo = y0 + 4 * K, clean_hi = n < ie ? n : ie;
+
+    // cp.async of row `row` into its ring slot (zero-filled where the row or a node lies outside
+    // the grid); every lane copies its own node pair
+    auto issue_row = [&](int row) {
+      const uint32_t slot = ring + (uint32_t)((row & (R - 1)) * G::ROWB);
+      const bool rin = row < n;
+      const size_t q = (size_t)(rin ? row : 0) * n + (in0 ? x : 0);
+      if (even) {
+        cp_async_sz<16>(slot + lane * 16, src + q, rin && in0 ? 16u : 0u);
+        cp_async_sz<8>(slot + 512 + lane * 8, Pg + q, rin && in0 ? 8u : 0u);
+      } else {
+        const size_t q1 = (size_t)(rin ? row : 0) * n + (in1 ? x + 1 : 0);
+        cp_async_sz<8>(slot + lane * 16, src + q, rin && in0 ? 8u : 0u);
+        cp_async_sz<8>(slot + lane * 16 + 8, src + q1, rin && in1 ? 8u : 0u);
+        cp_async_sz<4>(slot + 512 + lane * 8, Pg + q, rin && in0 ? 4u : 0u);
+        cp_async_sz<4>(slot + 512 + lane * 8 + 4, Pg + q1, rin && in1 ? 4u : 0u);
+      }
+    };
+
+    StreamWin<W> w;
+#pragma unroll
+    for (int s = 0; s < W; ++s) {
+      w.uX[s] = w.uY[s] = w.pc[s] = w.aX[s] = w.aY[s] = f2(0.f, 0.f);
+      w.t2X[s] = w.t2Y[s] = w.t3X[s] = w.t3Y[s] = w.t4X[s] = w.t4Y[s] = f2(0.f, 0.f);
+    }
+
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      if (ib + d < ie) issue_row(ib + d);
+      async_commit();
+    }
+
+    // One iteration of the wavefront at row i; P = (i - ib) mod W.  CHECK: decide per stage whether
+    // its row is needed by this segment (skip it otherwise) and zero stage values of rows beyond
+    // the grid (rows before the grid keep the zeros the windows start with).
+    auto iter = [&](int i, auto Pc, auto CHECKc) {
+      constexpr int P = decltype(Pc)::value;
+      constexpr bool CHECK = decltype(CHECKc)::value;
+      // row i: wait for its copy, move it into the window, prefetch row i + D
+      cp_async_wait_group<D - 1>();
+      {
+        const unsigned char* rs = ring_g + (i & (R - 1)) * G::ROWB;
+        const float4 v = *reinterpret_cast<const float4*>(rs + lane * 16);
+        const float2 p = *reinterpret_cast<const float2*>(rs + 512 + lane * 8);
+        w.uX[P] = f2(v.x, v.z);
+        w.uY[P] = f2(v.y, v.w);
+        w.pc[P] = mul2(c.c12, p);
+      }
+      if (i + D < ie) issue_row(i + D);
+      async_commit();
+
+      // stage 1 at row i - K: input u, output t2 = u + q1, a = q1
+      {
+        constexpr int C = ((P - K) % W + W) % W;
+        const int r = i - K;
+        bool run = true;
+        if (CHECK) {
+          if (r >= n) { w.t2X[C] = w.t2Y[C] = f2(0.f, 0.f); run = false; }
+          else run = r >= 0 && r >= y0 - 3 * K && r < y1 + 3 * K;
+        }
+        if (run) {
+          float2 qX, qY;
+          stream_slope<K, W, C>(w.uX, w.uY, w.pc[C], c, qX, qY);
+          w.aX[C] = qX;
+          w.aY[C] = qY;
+          w.t2X[C] = add2(w.uX[C], qX);
+          w.t2Y[C] = add2(w.uY[C], qY);
+        }
+      }
+      // stage 2 at row i - 2K: input t2, output t3 = u + q2, a += 2 q2
+      {
+        constexpr int C = ((P - 2 * K) % W + W) % W;
+        const int r = i - 2 * K;
+        bool run = true;
+        if (CHECK) {
+          if (r >= n) { w.t3X[C] = w.t3Y[C] = f2(0.f, 0.f); run = false; }
+          else run = r >= 0 && r >= y0 - 2 * K && r < y1 + 2 * K;
+        }
+        if (run) {
+          float2 qX, qY;
+          stream_slope<K, W, C>(w.t2X, w.t2Y, w.pc[C], c, qX, qY);
+          w.aX[C] = fma2(c.two, qX, w.aX[C]);
+          w.aY[C] = fma2(c.two, qY, w.aY[C]);
+          w.t3X[C] = add2(w.uX[C], qX);
+          w.t3Y[C] = add2(w.uY[C], qY);
+        }
+      }
+      // stage 3 at row i - 3K: input t3, output t4 = u + 2 q3, a += 2 q3
+      {
+        constexpr int C = ((P - 3 * K) % W + W) % W;
+        const int r = i - 3 * K;
+        bool run = true;
+        if (CHECK) {
+          if (r >= n) { w.t4X[C] = w.t4Y[C] = f2(0.f, 0.f); run = false; }
+          else run = r >= 0 && r >= y0 - K && r < y1 + K;
+        }
+        if (run) {
+          float2 qX, qY;
+          stream_slope<K, W, C>(w.t3X, w.t3Y, w.pc[C], c, qX, qY);
+          w.aX[C] = fma2(c.two, qX, w.aX[C]);
+          w.aY[C] = fma2(c.two, qY, w.aY[C]);
+          w.t4X[C] = fma2(c.two, qX, w.uX[C]);
+          w.t4Y[C] = fma2(c.two, qY, w.uY[C]);
+        }
+      }
+      // stage 4 at row i - 4K: input t4; u' = u + (q1 + 2 q2 + 2 q3 + q4) / 3, stored
+      {
+        constexpr int C = ((P - 4 * K) % W + W) % W;
+        const int r = i - 4 * K;
+        bool run = true;
+        if (CHECK) run = r >= y0 && r < y1 && r < n;
+        if (run) {
+          float2 qX, qY;
+          stream_slope<K, W, C>(w.t4X, w.t4Y, w.pc[C], c, qX, qY);
+          const float2 nX = fma2(c.third, add2(w.aX[C], qX), w.uX[C]);
+          const float2 nY = fma2(c.third, add2(w.aY[C], qY), w.uY[C]);
+          const size_t q = (size_t)r * n + x;
+          if (even) {
+            if (out0) *reinterpret_cast<float4*>(dst + q) = make_float4(nX.x, nY.x, nX.y, nY.y);
+          } else {
+            if (out0) dst[q] = f2(nX.x, nY.x);
+            if (out1) dst[q + 1] = f2(nX.y, nY.y);
+          }
+        }
+      }
+    };
+
+    for (int b = ib; b < ie; b += W) {
+      if (b >= clean_lo && b + W <= clean_hi) {
+        StaticFor<0, W>::run([&](auto Pc) { iter(b + decltype(Pc)::value, Pc, std::false_type{}); });
+      } else {
+        StaticFor<0, W>::run([&](auto Pc) {
+          if (b + decltype(Pc)::value < ie) iter(b + decltype(Pc)::value, Pc, std::true_type{});
+        });
+      }
+    }
+    cp_async_wait_group<0>();
+  }
+
+  // every warp of the launch is done taking items: the last one resets the counter
+  if (lane == 0) {
+    __threadfence();
+    const unsigned done = atomicAdd(&counter[1], 1u);
+    if (done == gridDim.x * G::WARPS - 1) {
+      counter[0] = 0u;
+      counter[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
+}  // namespace nlsg

@@ -122,4 +122,12 @@ struct TileItem {
   int tile;
 };
 
+// One work item of the streaming 2-D step: the strip of 64 columns starting at x0 of instance
+// inst, whose columns [ox0, ox1) it writes, over the rows [y0, y1).  Grid sides are below 65536
+// (n * n must fit an int).
+struct StripItem {
+  int inst;
+  uint16_t x0, ox0, ox1, y0, y1, pad;
+};
+
 }  // namespace nlsg
