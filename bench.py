@@ -142,6 +142,19 @@ def dist_init():
     return ws, rank, local
 
 
+def launch_ranks(n: int) -> int:
+    """--gpus N outside torchrun: start N ranks of this command (one per GPU, rendezvous on
+    127.0.0.1) with torch.distributed.run and return its exit status; rank 0 prints the line."""
+    import socket
+    sk = socket.socket()
+    sk.bind(("127.0.0.1", 0))
+    port = sk.getsockname()[1]
+    sk.close()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
 def barrier(ws):
     if ws > 1:
         import torch.distributed as dist
@@ -209,7 +222,7 @@ def run_reference(args):
     value = float(np.mean(rates))
     sample = f"every 4th of the 512 mixed instances ({len(specs)} solves), {steps} RK4 steps each, float32"
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times) * 1e3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex64",
         "data": "synthetic (seeded)",
@@ -599,6 +612,12 @@ def main():
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
                     help="choose kernel variants per size with the batch-throughput autotuner")
     args = ap.parse_args()
+    ws_env = os.environ.get("WORLD_SIZE")
+    if ws_env is None and args.gpus > 1:
+        return launch_ranks(args.gpus)
+    if ws_env is not None and int(ws_env) != args.gpus:
+        print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={ws_env}; launch one rank per GPU", file=sys.stderr)
+        return 2
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "precision2d":

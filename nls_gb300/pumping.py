@@ -102,7 +102,8 @@ class GaussianPumping(AbstractPumping):
         return self.power * np.exp(-r2 / (2.0 * self.variation ** 2))
 
     def __repr__(self):
-        return f"{self.power} exp(-{1.0 / (2.0 * self.variation ** 2)} ((x - {self.x0})^2 - (y - {self.y0})^2))"
+        return (f"{type(self).__name__}(power={self.power!r}, x0={self.x0!r}, y0={self.y0!r}, "
+                f"variation={self.variation!r})")
 
 
 class GaussianPumping1D(GaussianPumping):
@@ -133,7 +134,9 @@ class GaussianRingPumping2D(AbstractPumping):
         return self.pumping(r, t)
 
     def __repr__(self):
-        return "<class GaussianRingPumping2D(AbstractPumping)>"
+        g = self.pumping.lhs
+        return (f"GaussianRingPumping2D(power={g.power!r}, x0={self.x0!r}, y0={self.y0!r}, "
+                f"variation={g.variation!r}, radius={g.x0!r})")
 
 
 class GaussianElipticPumping2D(AbstractPumping):
@@ -148,7 +151,8 @@ class GaussianElipticPumping2D(AbstractPumping):
         return self.power * (np.exp(-(re - rp) ** 2 / (2 * self.var)) + np.exp(-(re + rp) ** 2 / (2 * self.var)))
 
     def __repr__(self):
-        return "<class GaussianElipticPumping2D(AbstractPumping)>"
+        return (f"GaussianElipticPumping2D(power={self.power!r}, x0={self.x0!r}, y0={self.y0!r}, "
+                f"variation={self.var!r}, a={self.a!r}, b={self.b!r})")
 
 
 class RectangularPumping1D(AbstractPumping):
@@ -163,7 +167,7 @@ class RectangularPumping1D(AbstractPumping):
         return out
 
     def __repr__(self):
-        return f"{self.power} * (\\theta(x - {self.x0 + self.width / 2.0}) - \\theta({self.x0 - self.width / 2.0} - x))"
+        return f"RectangularPumping1D(power={self.power!r}, x0={self.x0!r}, width={self.width!r})"
 
 
 class RectangularRingPumping1D(OpSumPumping):

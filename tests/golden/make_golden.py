@@ -113,7 +113,9 @@ def restatement_fixtures() -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("NLS_REFERENCE_ROOT"), required="NLS_REFERENCE_ROOT" not in os.environ,
+                    help="checkout of daskol/nls whose test/test_nls.f95 holds the known-answer tests "
+                         "(or set NLS_REFERENCE_ROOT)")
     args = ap.parse_args()
     kat = kat_from_reference(args.reference)
     with open(os.path.join(HERE, "kat_test_nls_f95.json"), "w") as f:

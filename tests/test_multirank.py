@@ -66,3 +66,34 @@ def test_reference_arm_nonzero_rank_does_no_work(monkeypatch):
         steps, warmup = 3, 3
     assert bench.run_reference(A()) == 0
     assert calls == []
+
+
+def test_bench_gpus_two_launches_two_ranks():
+    """`bench.py --gpus 2` outside torchrun starts two ranks itself (gloo on a CPU host); the
+    reference arm runs on rank 0 only and reports the run's world size."""
+    import json
+    import subprocess
+    import sys
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("runs the gloo path; a GPU box uses NCCL")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--impl", "reference",
+                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=600, env=env,
+                       cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+
+
+def test_bench_refuses_mismatched_world_size():
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, WORLD_SIZE="3")
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--impl", "reference"],
+                       capture_output=True, text=True, timeout=120, env=env, cwd=root)
+    assert r.returncode == 2 and "WORLD_SIZE" in r.stderr
