@@ -117,6 +117,12 @@ int nls_chemical_potential_2d(nls_ctx* ctx, int dtype, double dx, int n, const d
 int nls_chemical_potential_device(nls_ctx* ctx, int dtype, const nls_problem* problem,
                                   const void* pumping_dev, const void* u_dev, double* mu_re,
                                   double* mu_im);
+/* Damping integral of a device state, as Solution.getDampingIntegral (nls/model.py:350-365): the
+ * rectangle rule of (n_res - 1) |u|^2 with the reservoir n_res = c12 P / (c13 + c14 |u|^2), weighted
+ * by 2 pi r dx on r = linspace(0, n dx, n) in 1-D and by dx^2 in 2-D; FP64.  problem supplies dim,
+ * n, dx and coeffs; pumping_dev has the state's precision.  Blocks until done. */
+int nls_damping_integral_device(nls_ctx* ctx, int dtype, const nls_problem* problem,
+                                const void* pumping_dev, const void* u_dev, double* integral);
 /* sum |u|^2 over count nodes and the number of non-finite components; blocks until done. */
 int nls_norm_device(nls_ctx* ctx, int dtype, int64_t count, const void* u_dev, double* sum_sq,
                     int64_t* nonfinite);

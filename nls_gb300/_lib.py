@@ -74,6 +74,7 @@ SIGNATURES = {
     "nls_chemical_potential_2d": (_i, [_p, _i, _d, _i, _p, _p, _p, _pd]),
     "nls_chemical_potential_device": (_i, [_p, _i, _pp, _p, _p, _pd, _pd]),
     "nls_norm_device": (_i, [_p, _i, _i64, _p, _pd, _pi64]),
+    "nls_damping_integral_device": (_i, [_p, _i, _pp, _p, _p, _pd]),
     "nls_density_error_device": (_i, [_p, _i, _i64, _p, _p, _p, _d, _d, _d, _pd, _pd]),
     "nls_batch_create": (_i, [_p, _i, _i, _pp, ctypes.POINTER(_p)]),
     "nls_batch_set": (_i, [_p, _i, _p, _p]),

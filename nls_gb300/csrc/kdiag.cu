@@ -92,6 +92,33 @@ __global__ void __launch_bounds__(kDiagThreads) k_relerr(long long n, const void
     for (int k = 0; k < 4; ++k) part[blockIdx.x * 4 + k] = v[k];
 }
 
+// Damping integral of Solution.getDampingIntegral (nls/model.py:350-365): the rectangle rule of
+// (n_res - 1) |u|^2 with n_res = c12 P / (c13 + c14 |u|^2), weighted by w_i = 2 pi r_i dx on the
+// radial grid r_i = i * r_step (r_step = n dx / (n - 1), the spacing of linspace(0, n dx, n)) when
+// radial, else by dx^2.
+template <typename T>
+__global__ void __launch_bounds__(kDiagThreads) k_damping(long long n, const void* __restrict__ u_,
+                                                          const void* __restrict__ P_, int radial,
+                                                          double r_step, double dx, double c12, double c13,
+                                                          double c14, double* __restrict__ part) {
+  typedef typename C2<T>::type C;
+  __shared__ double sm[32 * 1];
+  const C* u = reinterpret_cast<const C*>(u_);
+  const T* P = reinterpret_cast<const T*>(P_);
+  const double two_pi = 6.283185307179586476925286766559;
+  double v[1] = {0.0};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const C a = u[i];
+    const double d = (double)a.x * (double)a.x + (double)a.y * (double)a.y;
+    const double res = c12 * (double)P[i] / (c13 + c14 * d);
+    const double w = radial ? two_pi * ((double)i * r_step) * dx : dx * dx;
+    v[0] += (res - 1.0) * d * w;
+  }
+  block_sum<1>(v, sm);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
 // Sum the per-block partials in a fixed order (one warp per value).
 __global__ void k_final(const double* __restrict__ part, int nblocks, int nv, double* __restrict__ out) {
   const int k = threadIdx.x >> 5;
@@ -123,6 +150,16 @@ cudaError_t diag_mu(int dtype, long long n, const void* u, const void* v, int mo
   if (dtype == NLS_C128) k_mu<double><<<nb, kDiagThreads, 0, st>>>(n, u, v, mode, dx, part);
   else k_mu<float><<<nb, kDiagThreads, 0, st>>>(n, u, v, mode, dx, part);
   k_final<<<1, 32 * 3, 0, st>>>(part, nb, 3, out);
+  return cudaGetLastError();
+}
+
+cudaError_t diag_damping(int dtype, long long n, const void* u, const void* P, int radial, double r_step,
+                         double dx, double c12, double c13, double c14, double* part, double* out,
+                         cudaStream_t st) {
+  const int nb = blocks_for(n);
+  if (dtype == NLS_C128) k_damping<double><<<nb, kDiagThreads, 0, st>>>(n, u, P, radial, r_step, dx, c12, c13, c14, part);
+  else k_damping<float><<<nb, kDiagThreads, 0, st>>>(n, u, P, radial, r_step, dx, c12, c13, c14, part);
+  k_final<<<1, 32, 0, st>>>(part, nb, 1, out);
   return cudaGetLastError();
 }
 

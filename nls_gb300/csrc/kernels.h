@@ -109,6 +109,11 @@ cudaError_t diag_norm(int dtype, long long n, const void* u, int weight_mode, do
                       double* d_partials, double* d_out, cudaStream_t st);
 cudaError_t diag_mu(int dtype, long long n, const void* u, const void* v, int weight_mode,
                     double dx, double* d_partials, double* d_out, cudaStream_t st);
+// damping: out[0] = sum w_i (c12 P_i / (c13 + c14 |u_i|^2) - 1) |u_i|^2, w_i = 2 pi (i r_step) dx
+// (radial) or dx^2
+cudaError_t diag_damping(int dtype, long long n, const void* u, const void* P, int radial, double r_step,
+                         double dx, double c12, double c13, double c14, double* d_partials, double* d_out,
+                         cudaStream_t st);
 cudaError_t diag_relerr(int dtype_a, long long n, const void* a, const void* b_c128,
                         const double* P, double c12, double c13, double c14, double* d_partials,
                         double* d_out, cudaStream_t st);

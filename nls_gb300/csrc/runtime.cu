@@ -246,6 +246,57 @@ static int solve_1d_dev(nls_ctx* ctx, int dtype, const nls_problem* pr, int64_t 
   return NLS_OK;
 }
 
+// Streaming 2-D step (complex64): ping-pong between the caller's buffer and one scratch buffer,
+// strip items over segments of the height that balances the grid's work over the GPU's warps.
+static int stream_grid(nls_ctx* ctx, int K, int n_items) {
+  const int occ = std::max(1, stream_2d_blocks_per_sm(K));
+  const int wpb = stream_2d_warps_per_block();
+  return std::max(1, std::min(ctx->sm_count * occ, (n_items + wpb - 1) / wpb));
+}
+static int64_t stream_slots(nls_ctx* ctx, int K) {
+  return (int64_t)ctx->sm_count * std::max(1, stream_2d_blocks_per_sm(K)) * stream_2d_warps_per_block();
+}
+
+static int solve_2d_stream(nls_ctx* ctx, const nls_problem* pr, const Stencil2D& op, const PhysD& ph,
+                           int64_t iters, const void* P, void* u) {
+  const int n = pr->n;
+  const size_t N = (size_t)n * n;
+  const size_t cb = align256(N * csize(NLS_C64));
+  CK(ctx, ctx->scratch.ensure(cb));
+  Inst2D I;
+  std::memset(&I, 0, sizeof(I));
+  I.u[0] = u; I.u[1] = ctx->scratch.p; I.P = P; I.n = n; I.tiles_x = 0; I.parity = 0;
+  I.steps = INT64_MAX; I.dt = pr->dt; I.ph = ph; I.op = op;
+  set_params(I);
+  std::vector<StripItem> items;
+  stream_items(0, n, op.K, stream_choose_ly({n}, op.K, stream_slots(ctx, op.K)), items);
+  stream_sort_items(items);
+  const int n_items = (int)items.size();
+  const size_t ib = align256(sizeof(Inst2D));
+  const size_t tb = align256(sizeof(StripItem) * n_items);
+  CK(ctx, ctx->desc.ensure(ib + tb + 256));
+  Inst2D* dI = (Inst2D*)ctx->desc.p;
+  StripItem* dT = (StripItem*)((char*)ctx->desc.p + ib);
+  unsigned* counter = (unsigned*)((char*)ctx->desc.p + ib + tb);
+  CK(ctx, cudaMemcpyAsync(dI, &I, sizeof(I), cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(dT, items.data(), sizeof(StripItem) * n_items, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned), ctx->stream));
+  const int grid = stream_grid(ctx, op.K, n_items);
+  const int S = 64;  // even: a replay returns the state to the caller's buffer
+  CK(ctx, replay(ctx, iters / S, [&]() -> cudaError_t {
+       for (int j = 0; j < S; ++j) {
+         cudaError_t e = launch_2d_stream(op.K, dI, dT, n_items, j, grid, counter, ctx->stream);
+         if (e) return e;
+       }
+       return cudaSuccess;
+     }));
+  const int64_t rem = iters % S;
+  for (int64_t j = 0; j < rem; ++j) CK(ctx, launch_2d_stream(op.K, dI, dT, n_items, (int)j, grid, counter, ctx->stream));
+  if (rem & 1) CK(ctx, cudaMemcpyAsync(u, ctx->scratch.p, N * csize(NLS_C64), cudaMemcpyDeviceToDevice, ctx->stream));
+  ctx->launches += iters;
+  return NLS_OK;
+}
+
 static int solve_2d_dev(nls_ctx* ctx, int dtype, const nls_problem* pr, int64_t iters,
                         const void* P, void* u) {
   Stencil2D op;
@@ -277,6 +328,7 @@ static int solve_2d_dev(nls_ctx* ctx, int dtype, const nls_problem* pr, int64_t 
     ctx->launches += 4 * iters;
     return NLS_OK;
   }
+  if (shape == TILE_STREAM) return solve_2d_stream(ctx, pr, op, ph, iters, P, u);
   // fused: ping-pong between the caller's buffer and one scratch buffer
   const int tx = tile_out_x(shape, op.K), ty = tile_out_y(shape, op.K);
   const int tiles_x = (n + tx - 1) / tx, tiles_y = (n + ty - 1) / ty;
@@ -499,6 +551,11 @@ struct Group2D {
   int n_items = 0;
   bool tma = false;
   char* maps = nullptr;    // 3 tensor maps per member (TMA path)
+  // streaming step (TILE_STREAM): strip items of every member, longest first, and the
+  // launch-wide item counter
+  std::vector<StripItem> sitems_h;
+  StripItem* sitems = nullptr;
+  unsigned* counter = nullptr;
 };
 
 struct Member {
@@ -570,7 +627,12 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
       M.kind = shape > 0 ? 2 : 3;
       if (M.kind == 2) {
         auto k = std::make_pair(M.op2.K, shape);
-        if (!key2.count(k)) { key2[k] = (int)b->g2.size(); b->g2.push_back(Group2D{M.op2.K, shape, 0, {}, nullptr, nullptr, 0, false, nullptr}); }
+        if (!key2.count(k)) {
+          key2[k] = (int)b->g2.size();
+          Group2D G;
+          G.K = M.op2.K; G.shape = shape; G.grid = 0;
+          b->g2.push_back(G);
+        }
         M.group = key2[k];
         b->g2[M.group].idx.push_back(i);
       }
@@ -604,14 +666,27 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
   for (size_t g = 0; g < b->g2.size(); ++g) {
     Group2D& G = b->g2[g];
     int items = 0;
-    for (int i : G.idx) {
-      const int tx = tile_out_x(G.shape, G.K), ty = tile_out_y(G.shape, G.K), n = b->m[i].pr.n;
-      items += ((n + tx - 1) / tx) * ((n + ty - 1) / ty);
+    size_t item_bytes = 0;
+    if (G.shape == TILE_STREAM) {
+      std::vector<int> ns;
+      for (int i : G.idx) ns.push_back(b->m[i].pr.n);
+      const int ly = stream_choose_ly(ns, G.K, stream_slots(ctx, G.K));
+      G.sitems_h.clear();
+      for (size_t k = 0; k < G.idx.size(); ++k) stream_items((int)k, ns[k], G.K, ly, G.sitems_h);
+      stream_sort_items(G.sitems_h);
+      items = (int)G.sitems_h.size();
+      item_bytes = align256(sizeof(StripItem) * std::max(1, items)) + 256;   // + the item counter
+    } else {
+      for (int i : G.idx) {
+        const int tx = tile_out_x(G.shape, G.K), ty = tile_out_y(G.shape, G.K), n = b->m[i].pr.n;
+        items += ((n + tx - 1) / tx) * ((n + ty - 1) / ty);
+      }
+      item_bytes = align256(sizeof(TileItem) * std::max(1, items));
     }
     G.n_items = items;
     g2off[g] = off; off += align256(sizeof(Inst2D) * G.idx.size());
-    g2items[g] = off; off += align256(sizeof(TileItem) * std::max(1, items));
-    g2maps.push_back(off); off += align256(tma_map_bytes() * G.idx.size());
+    g2items[g] = off; off += item_bytes;
+    g2maps.push_back(off); off += G.shape == TILE_STREAM ? 0 : align256(tma_map_bytes() * G.idx.size());
   }
   b->mem_bytes = std::max<size_t>(off, 256);
   CK(ctx, cudaMalloc(&b->mem, b->mem_bytes));
@@ -627,6 +702,16 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
   for (size_t g = 0; g < b->g2.size(); ++g) {
     Group2D& G = b->g2[g];
     G.d = (Inst2D*)(b->mem + g2off[g]);
+    if (G.shape == TILE_STREAM) {
+      G.sitems = (StripItem*)(b->mem + g2items[g]);
+      G.counter = (unsigned*)(b->mem + g2items[g] + align256(sizeof(StripItem) * std::max(1, G.n_items)));
+      if (G.n_items)
+        CK(ctx, cudaMemcpyAsync(G.sitems, G.sitems_h.data(), sizeof(StripItem) * G.n_items, cudaMemcpyHostToDevice,
+                                ctx->stream));
+      G.tma = false;
+      G.grid = stream_grid(ctx, G.K, std::max(1, G.n_items));
+      continue;
+    }
     G.items = (TileItem*)(b->mem + g2items[g]);
     std::vector<TileItem> items;
     items.reserve(G.n_items);
@@ -688,7 +773,8 @@ static int batch_descriptors(nls_batch* b, int64_t steps) {
       std::memset(&I, 0, sizeof(I));
       const int tx = tile_out_x(G.shape, G.K);
       I.u[0] = M.u[0]; I.u[1] = M.u[1]; I.P = M.P; I.n = M.pr.n;
-      I.tiles_x = (M.pr.n + tx - 1) / tx; I.parity = M.parity; I.steps = INT64_MAX; I.dt = M.pr.dt;
+      I.tiles_x = G.shape == TILE_STREAM ? 0 : (M.pr.n + tx - 1) / tx;
+      I.parity = M.parity; I.steps = INT64_MAX; I.dt = M.pr.dt;
       I.ph = phys_of(M.pr.coeffs); I.op = M.op2;
       I.tmap = G.tma ? G.maps + k * tma_map_bytes() : nullptr;
       set_params(I);
@@ -717,9 +803,11 @@ static cudaError_t batch_sequence(nls_batch* b, int64_t steps) {
   }
   for (int64_t j = 0; j < steps; ++j) {
     for (auto& G : b->g2)
-      if ((e = G.tma ? launch_2d_fused_tma(G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream,
-                                           ctx->wait_flag)
-                     : launch_2d_fused(dtype, G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream)))
+      if ((e = G.shape == TILE_STREAM
+                   ? launch_2d_stream(G.K, G.d, G.sitems, G.n_items, (int)j, G.grid, G.counter, ctx->stream)
+               : G.tma ? launch_2d_fused_tma(G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream,
+                                             ctx->wait_flag)
+                       : launch_2d_fused(dtype, G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream)))
         return e;
     for (auto& M : b->m) {
       if (M.kind != 3) continue;
@@ -968,6 +1056,28 @@ NLS_API int nls_norm_device(nls_ctx* ctx, int dtype, int64_t count, const void* 
   *sum_sq = ctx->h_diag[0];
   if (nonfinite) *nonfinite = (int64_t)ctx->h_diag[1];
   return ctx->h_diag[1] > 0 ? fail(ctx, NLS_ERR_NONFINITE, "non-finite values in state") : NLS_OK;
+}
+
+NLS_API int nls_damping_integral_device(nls_ctx* ctx, int dtype, const nls_problem* pr, const void* pumping_dev,
+                                        const void* u_dev, double* integral) {
+  if (!ctx) return NLS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!pr || !pumping_dev || !u_dev || !integral) return fail(ctx, NLS_ERR_INVALID, "bad arguments");
+  if (dtype != NLS_C128 && dtype != NLS_C64) return fail(ctx, NLS_ERR_INVALID, "bad dtype");
+  if ((pr->dim != 1 && pr->dim != 2) || pr->n < 1 || !(pr->dx > 0.0)) return fail(ctx, NLS_ERR_INVALID, "dim 1 or 2, n >= 1, dx > 0");
+  CK(ctx, cudaSetDevice(ctx->device));
+  int st = diag_ensure(ctx);
+  if (st) return st;
+  const long long N = pr->dim == 1 ? (long long)pr->n : (long long)pr->n * pr->n;
+  const double r_step = pr->n > 1 ? (double)pr->n * pr->dx / (double)(pr->n - 1) : 0.0;
+  const double* c = pr->coeffs;
+  CK(ctx, diag_damping(dtype, N, u_dev, pumping_dev, pr->dim == 1 ? 1 : 0, r_step, pr->dx, c[11], c[12], c[13],
+                       (double*)ctx->diag.p, diag_out(ctx), ctx->stream));
+  CK(ctx, cudaMemcpyAsync(ctx->h_diag, diag_out(ctx), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->launches += 2;
+  *integral = ctx->h_diag[0];
+  return NLS_OK;
 }
 
 NLS_API int nls_density_error_device(nls_ctx* ctx, int dtype, int64_t count, const void* u_dev,
@@ -1266,9 +1376,14 @@ NLS_API int nls_pool_admit(nls_pool* p, const nls_problem* problem, const void* 
     if (!tile_supported(S.shape, p->dtype)) return fail(ctx, NLS_ERR_INVALID, "2-D shape not servable");
     S.kind = 2;
     S.N = (size_t)S.pr.n * S.pr.n;
-    const int tx = tile_out_x(S.shape, S.K), ty = tile_out_y(S.shape, S.K);
-    S.tiles_x = (S.pr.n + tx - 1) / tx;
-    S.ntiles = S.tiles_x * ((S.pr.n + ty - 1) / ty);
+    if (S.shape == TILE_STREAM) {
+      S.tiles_x = 0;    // strip items are made per chunk over the pool's current mix
+      S.ntiles = 0;
+    } else {
+      const int tx = tile_out_x(S.shape, S.K), ty = tile_out_y(S.shape, S.K);
+      S.tiles_x = (S.pr.n + tx - 1) / tx;
+      S.ntiles = S.tiles_x * ((S.pr.n + ty - 1) / ty);
+    }
   }
   int free_slot = -1;
   for (size_t i = 0; i < p->slots.size(); ++i)
@@ -1289,7 +1404,7 @@ NLS_API int nls_pool_admit(nls_pool* p, const nls_problem* problem, const void* 
   S.remaining = steps;
   S.parity = 0;
   if (S.done) S.finish_seq = ++p->seq;
-  if (S.kind == 2 && tma_eligible(p->dtype, S.pr.n, S.u[0], S.u[1], S.P)) {
+  if (S.kind == 2 && S.shape != TILE_STREAM && tma_eligible(p->dtype, S.pr.n, S.u[0], S.u[1], S.P)) {
     std::vector<unsigned char> buf(tma_map_bytes() + 128);
     unsigned char* hm = (unsigned char*)(((uintptr_t)buf.data() + 127) & ~(uintptr_t)127);
     if (tma_encode_2d(S.shape, S.K, S.pr.n, S.u[0], S.u[1], S.P, hm) == 0) {
@@ -1328,19 +1443,44 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
   }
   if (finished) *finished = 0;
   if (g1.empty() && g2.empty()) return NLS_OK;
-  // descriptor image: all groups back to back
+  // work items of each 2-D group: tiles, or strip items over the group's current mix
+  std::vector<std::vector<StripItem>> sitems(g2.size());
+  {
+    size_t gi = 0;
+    for (auto& kv : g2) {
+      const int K = std::get<0>(kv.first), shape = std::get<1>(kv.first);
+      if (shape == TILE_STREAM) {
+        std::vector<int> ns;
+        for (int i : kv.second) ns.push_back(p->slots[i].pr.n);
+        const int ly = stream_choose_ly(ns, K, stream_slots(ctx, K));
+        for (size_t k = 0; k < ns.size(); ++k) stream_items((int)k, ns[k], K, ly, sitems[gi]);
+        stream_sort_items(sitems[gi]);
+      }
+      ++gi;
+    }
+  }
+  // descriptor image: all groups back to back (a streaming group's item counter is part of the
+  // image and uploads as zero)
   size_t bytes = 0;
   for (auto& kv : g1) bytes += align256(sizeof(Inst1D) * kv.second.size());
-  for (auto& kv : g2) {
-    int items = 0;
-    for (int i : kv.second) items += p->slots[i].ntiles;
-    bytes += align256(sizeof(Inst2D) * kv.second.size()) + align256(sizeof(TileItem) * items) +
-             align256(tma_map_bytes() * kv.second.size());
+  {
+    size_t gi = 0;
+    for (auto& kv : g2) {
+      if (std::get<1>(kv.first) == TILE_STREAM) {
+        bytes += align256(sizeof(Inst2D) * kv.second.size()) + align256(sizeof(StripItem) * std::max<size_t>(1, sitems[gi].size())) + 256;
+      } else {
+        int items = 0;
+        for (int i : kv.second) items += p->slots[i].ntiles;
+        bytes += align256(sizeof(Inst2D) * kv.second.size()) + align256(sizeof(TileItem) * items) +
+                 align256(tma_map_bytes() * kv.second.size());
+      }
+      ++gi;
+    }
   }
   p->h_desc.assign(bytes, 0);
   CK(ctx, p->d_desc.ensure(bytes));
   struct L1 { int K, cl, seg, count; size_t off; };
-  struct L2 { int K, shape, n_items, grid; size_t off, off_items; bool tma; };
+  struct L2 { int K, shape, n_items, grid; size_t off, off_items, off_counter; bool tma; };
   std::vector<L1> l1;
   std::vector<L2> l2;
   size_t off = 0;
@@ -1359,16 +1499,21 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
     l1.push_back(L1{kv.first.first, kv.first.second, seg, (int)kv.second.size(), off});
     off += align256(sizeof(Inst1D) * kv.second.size());
   }
+  size_t gi = 0;
   for (auto& kv : g2) {
     const int K = std::get<0>(kv.first), shape = std::get<1>(kv.first);
     const bool tma = std::get<2>(kv.first) != 0;
+    const bool stream = shape == TILE_STREAM;
     Inst2D* h = (Inst2D*)(p->h_desc.data() + off);
     const size_t ioff = off + align256(sizeof(Inst2D) * kv.second.size());
-    TileItem* it = (TileItem*)(p->h_desc.data() + ioff);
     int items = 0;
-    for (int i : kv.second) items += p->slots[i].ntiles;
-    const size_t moff = ioff + align256(sizeof(TileItem) * items);
-    items = 0;
+    if (stream) items = (int)sitems[gi].size();
+    else for (int i : kv.second) items += p->slots[i].ntiles;
+    const size_t moff = ioff + (stream ? align256(sizeof(StripItem) * std::max(1, items))
+                                       : align256(sizeof(TileItem) * items));
+    TileItem* it = (TileItem*)(p->h_desc.data() + ioff);
+    if (stream && items) std::memcpy(p->h_desc.data() + ioff, sitems[gi].data(), sizeof(StripItem) * items);
+    int q_items = 0;
     for (size_t k = 0; k < kv.second.size(); ++k) {
       const Slot& S = p->slots[kv.second[k]];
       Inst2D& I = h[k];
@@ -1380,12 +1525,19 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
         std::memcpy(p->h_desc.data() + moff + k * tma_map_bytes(), S.maps.data(), tma_map_bytes());
         I.tmap = (char*)p->d_desc.p + moff + k * tma_map_bytes();
       }
-      for (int q = 0; q < S.ntiles; ++q) it[items++] = TileItem{(int)k, q};
+      if (!stream)
+        for (int q = 0; q < S.ntiles; ++q) it[q_items++] = TileItem{(int)k, q};
     }
-    const int occ = tma ? fused_2d_tma_blocks_per_sm(K, shape) : fused_2d_blocks_per_sm(dtype, K, shape);
-    const int grid = std::max(1, std::min(items, ctx->sm_count * std::max(1, occ)));
-    l2.push_back(L2{K, shape, items, grid, off, ioff, tma});
-    off = moff + align256(tma_map_bytes() * kv.second.size());
+    int grid;
+    if (stream) {
+      grid = stream_grid(ctx, K, std::max(1, items));
+    } else {
+      const int occ = tma ? fused_2d_tma_blocks_per_sm(K, shape) : fused_2d_blocks_per_sm(dtype, K, shape);
+      grid = std::max(1, std::min(items, ctx->sm_count * std::max(1, occ)));
+    }
+    l2.push_back(L2{K, shape, items, grid, off, ioff, moff, tma});
+    off = moff + (stream ? 256 : align256(tma_map_bytes() * kv.second.size()));
+    ++gi;
   }
   char* d = (char*)p->d_desc.p;
   CK(ctx, cudaMemcpyAsync(d, p->h_desc.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
@@ -1400,10 +1552,15 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
   for (int64_t j = 0; j < max_steps; ++j)
     for (auto& L : l2) {
       const Inst2D* dI = (const Inst2D*)(d + L.off);
-      const TileItem* dT = (const TileItem*)(d + L.off_items);
-      CK(ctx, L.tma ? launch_2d_fused_tma(L.K, L.shape, dI, dT, L.n_items, (int)j, L.grid, ctx->stream,
-                                          ctx->wait_flag)
-                    : launch_2d_fused(dtype, L.K, L.shape, dI, dT, L.n_items, (int)j, L.grid, ctx->stream));
+      if (L.shape == TILE_STREAM) {
+        CK(ctx, launch_2d_stream(L.K, dI, (const StripItem*)(d + L.off_items), L.n_items, (int)j, L.grid,
+                                 (unsigned*)(d + L.off_counter), ctx->stream));
+      } else {
+        const TileItem* dT = (const TileItem*)(d + L.off_items);
+        CK(ctx, L.tma ? launch_2d_fused_tma(L.K, L.shape, dI, dT, L.n_items, (int)j, L.grid, ctx->stream,
+                                            ctx->wait_flag)
+                      : launch_2d_fused(dtype, L.K, L.shape, dI, dT, L.n_items, (int)j, L.grid, ctx->stream));
+      }
       ctx->launches += 1;
     }
   if (!l1.empty()) {

@@ -101,6 +101,22 @@ def chemical_potential(u: torch.Tensor, P: torch.Tensor, *, dx: float, coeffs) -
     return complex(re.value, im.value)
 
 
+def damping_integral(u: torch.Tensor, P: torch.Tensor, *, dx: float, coeffs) -> float:
+    """FP64 damping integral of a device state, as Solution.getDampingIntegral (nls/model.py:350-365):
+    rectangle rule of (n - 1)|u|^2 with n = c12 P / (c13 + c14 |u|^2), radial weight 2 pi r dx on
+    linspace(0, n dx, n) in 1-D, dx^2 in 2-D."""
+    ctx = context(u.device.index or 0)
+    ext = _ext_stream(ctx)
+    ext.wait_stream(torch.cuda.current_stream(u.device))
+    pr = _lib.make_problem(u.dim(), u.shape[0], 5, 0.0, dx, coeffs)
+    out = ctypes.c_double()
+    st = _lib.lib().nls_damping_integral_device(ctx.handle, _code_of(u), ctypes.byref(pr),
+                                                ctypes.c_void_p(P.data_ptr()), ctypes.c_void_p(u.data_ptr()),
+                                                ctypes.byref(out))
+    _lib.check(st, "nls_damping_integral_device", ctx.handle)
+    return out.value
+
+
 def density_errors(u: torch.Tensor, u_ref: torch.Tensor, P64: torch.Tensor, coeffs):
     """Relative L2 errors of |u|^2 and of the reservoir n against a complex128 reference."""
     if u_ref.dtype != torch.complex128 or P64.dtype != torch.float64:

@@ -192,3 +192,33 @@ def test_1d_c64_cluster_other_orders(gpu, oracle_lib, order):
     device.solve_(u, P, order=order, dt=s.dt, dx=s.dx, coeffs=s.coeffs, iters=600, variant=4)
     want32 = oracle_lib.solve(s.dt, s.dx, order, 600, s.pumping, s.coeffs, s.u0, dtype=np.float32)
     assert rel(u.cpu().numpy(), want32) <= 3e-5
+
+
+# ------------------------------------------------------------------ tools/check.py on device reductions
+
+@pytest.mark.parametrize("dim", [1, 2])
+def test_checks_fed_by_device_reductions_match_the_host_loop(gpu, dim):
+    """check_convergence / check_integral on the GPU-resident state and FP64 device reductions
+    against the reference's host loop (tools/check.py:33-37: setInitialSolution, solve(num_iters),
+    getChemicalPotential, getDampingIntegral) run through the same API."""
+    import copy
+    from nls_gb300 import checks
+    model = _config0_model(num_iters=400) if dim == 1 else _config1_model(num_nodes=72, num_iters=200)
+    sol = model.solve()
+    hist = checks.convergence_history(sol, num_steps=6, num_iters=25)
+    # the host loop of the reference, through Problem/Model/Solution and nls.native
+    m2 = copy.deepcopy(model)
+    prof = sol
+    eig, ints = [], []
+    for _ in range(6):
+        m2.setInitialSolution(prof.getSolution())
+        prof = m2.solve(25)
+        eig.append(m2.getChemicalPotential(prof.getSolution()))
+        ints.append(prof.getDampingIntegral())
+    eig = np.array(eig, dtype=complex)
+    np.testing.assert_allclose(hist["eigenvalues"], eig, rtol=1e-9, atol=0)
+    np.testing.assert_allclose(hist["integrals"], ints, rtol=1e-9, atol=1e-12)
+    assert checks.check_convergence(sol, num_steps=6, num_iters=25) == (np.std(eig) < checks.TOLERANCE)
+    di = checks.damping_integral(sol)
+    assert abs(di - sol.getDampingIntegral()) <= 1e-10 * max(1.0, abs(di))
+    assert checks.check_integral(sol) == (abs(sol.getDampingIntegral()) <= checks.TOLERANCE)

@@ -166,7 +166,7 @@ def _oracle_2d_pair(oracle_lib, s, order, iters):
 # n = 150: plain global loads (rows not 16-byte multiples); n = 152: the TMA tile path
 @pytest.mark.parametrize("n", [150, 152])
 @pytest.mark.parametrize("order", [3, 5])
-@pytest.mark.parametrize("variant", [-1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14])
+@pytest.mark.parametrize("variant", [-1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15])
 def test_2d_c64_vs_oracles(gpu, oracle_lib, order, variant, n):
     s = _spec_2d(n, order)
     iters = 400
@@ -244,7 +244,7 @@ def test_invalid_arguments_raise(gpu):
 # ------------------------------------------------------------------ resume, batch, pool
 
 @pytest.mark.parametrize("dim,variant,dtype", [(1, -1, np.complex128), (1, 0, np.complex64),
-                                               (2, 1, np.complex64), (2, 8, np.complex64),
+                                               (2, 1, np.complex64), (2, 8, np.complex64), (2, 15, np.complex64),
                                                (2, 0, np.complex128), (2, 3, np.complex128)])
 def test_resume_is_bitwise(gpu, dim, variant, dtype):
     """One solve of N steps equals k solves of N/k steps from the device-resident state."""
@@ -273,7 +273,7 @@ def _mixed_specs(dtype):
 
 
 @pytest.mark.parametrize("dtype,shape2d", [(np.complex64, -1), (np.complex64, 12), (np.complex64, 9),
-                                            (np.complex128, -1)])
+                                            (np.complex64, 15), (np.complex128, -1)])
 def test_batch_matches_single_solves(gpu, dtype, shape2d):
     from nls_gb300.batch import BatchSolver
     specs = _mixed_specs(dtype)
@@ -359,10 +359,11 @@ def test_batch_packed_layout_matches_per_instance(gpu, steps):
         b.set_packed(hP[:-1], hU)
 
 
-def test_pool_same_alone_and_in_the_mix(gpu):
+@pytest.mark.parametrize("variant2d", [-1, 15])
+def test_pool_same_alone_and_in_the_mix(gpu, variant2d):
     from nls_gb300 import workloads as w
     from nls_gb300.serve import Pool
-    target = w.mix_instance(3, 2)
+    target = w.mix_instance(3, 2, variant=variant2d)
     target1 = w.mix_instance(4, 1)
     alone = Pool(budget_bytes=1 << 30, chunk_steps=40)
     alone.admit(target, 123, 0)
@@ -371,7 +372,7 @@ def test_pool_same_alone_and_in_the_mix(gpu):
         alone.step()
     ra = dict([alone.take_with_state(), alone.take_with_state()])
     mix = Pool(budget_bytes=1 << 30, chunk_steps=40)
-    others = [w.mix_instance(20 + i, 1 + (i % 2)) for i in range(8)]
+    others = [w.mix_instance(20 + i, 1 + (i % 2), variant=variant2d if i % 2 else -1) for i in range(8)]
     for k, o in enumerate(others[:4]):
         mix.admit(o, 50 + 13 * k, 100 + k)
     mix.step()                                   # the target arrives while others run
@@ -392,7 +393,7 @@ def test_pool_same_alone_and_in_the_mix(gpu):
     assert np.array_equal(ra[0], rm[0])
     assert np.array_equal(ra[1], rm[1])
     # and equal to a plain single solve on the same kernel
-    want = _device_solve(gpu, target, 123, np.complex64, -1)
+    want = _device_solve(gpu, target, 123, np.complex64, variant2d)
     assert np.array_equal(rm[0], want)
 
 
@@ -430,9 +431,9 @@ def test_autotune_batch_mode_assigns_valid_variants(gpu, tmp_path, monkeypatch):
         assert np.array_equal(b.get(i), want.astype(np.complex64)), i
 
 
-@pytest.mark.parametrize("variant", [8, 10, 12])
+@pytest.mark.parametrize("variant", [8, 10, 12, 15])
 @pytest.mark.parametrize("order", [3, 5])
-@pytest.mark.parametrize("n", [5, 33, 64, 97, 200])
+@pytest.mark.parametrize("n", [5, 33, 64, 65, 97, 120, 121, 128, 200])
 def test_2d_c64_register_tiles_small_and_ragged(gpu, oracle_lib, variant, order, n):
     """Register-resident tiles on grids smaller than one region, odd sides (plain loads) and
     multiples of 4 (TMA), against the FP32 oracle."""
@@ -462,3 +463,15 @@ def test_tile_wait_timeout_is_reported_and_the_context_recovers(gpu, oracle_lib)
     got = _device_solve(gpu, s, 40, np.complex64, 10)
     want = oracle_lib.solve(s.dt, s.dx, 3, 40, s.pumping, s.coeffs, s.u0, dtype=np.float32)
     assert rel(got, want) <= 3e-5
+
+
+@pytest.mark.parametrize("order,n", [(3, 1000), (5, 1000), (3, 1030), (5, 515)])
+def test_2d_c64_stream_large_grids(gpu, oracle_lib, order, n):
+    """The streaming step on grids of many strips and row segments (segment warm-up and drain,
+    interior and edge strips, odd sides on the plain-load path) against the FP32 oracle."""
+    s = _spec_2d(n, order)
+    iters = 40
+    want32 = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float32,
+                              threads=os.cpu_count() or 1)
+    got = _device_solve(gpu, s, iters, np.complex64, 15)
+    assert rel(got, want32) <= 3e-5
