@@ -386,10 +386,84 @@ def run_serve(args):
                       "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": float(np.mean(lat) * 1e3),
                       "max_ms": float(np.max(lat) * 1e3), "wall_s": st["wall_s"],
                       "node_steps_per_s": st["node_steps_per_s"], "node_steps": st["node_steps"],
+                      "queue_p50_ms": st["queue_p50_ms"], "queue_p99_ms": st["queue_p99_ms"],
+                      "gpu_busy_frac": st["gpu_busy_frac"],
                       "plain_c128_sequential_node_steps_per_s": plain_ns / plain_s,
                       "plain_c128_sample": "24 requests of the stream solved one after another",
                       "autotuned_variants": tuned}))
     return 0
+
+
+# Algorithmic FP64 work of one node-step of the plain complex128 path (one RK4 step = four
+# right-hand sides + the RK4 combinations), counted per node and stage: the operator row (1-D
+# order 5: five complex-by-real multiply-adds, 20 flop; 2-D order 3: four neighbour sums and two
+# weights per component, 12 flop), |u|^2 (3), the reservoir (multiply, add, divide: 3), a and b
+# (4), the right-hand side (8) and the stage update plus accumulation (8).
+FP64_FLOP_PER_NODE_STEP = {(1, 5): 4 * (20 + 3 + 3 + 4 + 8 + 8), (2, 3): 4 * (12 + 3 + 3 + 4 + 8 + 8)}
+
+
+def measured_fp64_peak(dev):
+    """FP64 FLOP/s of cuBLAS DGEMM (4096^3, best of 5) on this GPU: the FP64 denominator."""
+    import torch
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize(dev)
+    best = 1e9
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return 2.0 * 4096 ** 3 / best
+
+
+def plain_config_leg(spec, steps, dev, fp64_peak, threads):
+    """One plain complex128 solve of a configuration, device-timed on resident tensors (CUDA events
+    on the library's stream, after one warm-up solve), and end to end through the f2py-shaped
+    call (host arrays in, host array out); relative L2 against the FP64 oracle outside the timed
+    regions."""
+    import torch
+    from nls_gb300 import device as ndev
+    from nls_gb300.native import nls
+    from oracle import oracle
+    u0 = np.asarray(spec.u0).T if spec.dim == 2 else np.asarray(spec.u0)
+    P = np.asarray(spec.pumping).T if spec.dim == 2 else np.asarray(spec.pumping)
+    Pt = torch.tensor(np.ascontiguousarray(P), dtype=torch.float64, device=dev)
+    kw = dict(order=spec.order, dt=spec.dt, dx=spec.dx, coeffs=spec.coeffs)
+    u = torch.tensor(np.ascontiguousarray(u0), dtype=torch.complex128, device=dev)
+    ndev.solve_(u, Pt, iters=steps, **kw)                         # warm-up
+    u = torch.tensor(np.ascontiguousarray(u0), dtype=torch.complex128, device=dev)
+    ext = ndev.stream(dev.index or 0)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    ndev.solve_(u, Pt, iters=steps, **kw)
+    e1.record(ext)
+    e1.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    t0 = time.perf_counter()
+    fn = nls.solve_nls if spec.dim == 1 else nls.solve_nls_2d
+    got = fn(spec.dt, spec.dx, spec.order, steps, spec.pumping, spec.coeffs, spec.u0)
+    e2e_sec = time.perf_counter() - t0
+    want = oracle.solve(spec.dt, spec.dx, spec.order, steps, spec.pumping, spec.coeffs, spec.u0, dtype=np.float64,
+                        threads=threads)
+    rel = float(np.linalg.norm(got - want) / np.linalg.norm(want))
+    dev_rel = float(np.linalg.norm((u.cpu().numpy().T if spec.dim == 2 else u.cpu().numpy()) - want)
+                    / np.linalg.norm(want))
+    ns = float(spec.nodes) * steps
+    flop = FP64_FLOP_PER_NODE_STEP.get((spec.dim, spec.order))
+    out = {"us_per_step": sec * 1e6 / steps, "node_steps_per_s": ns / sec, "seconds": sec,
+           "e2e_node_steps_per_s": ns / e2e_sec, "rel_l2_vs_fp64_oracle": max(rel, dev_rel)}
+    if flop and fp64_peak:
+        achieved = ns * flop / sec
+        out["fp64"] = {"flop_per_node_step": flop, "achieved_tflops": achieved / 1e12,
+                       "peak_tflops": fp64_peak / 1e12, "frac": achieved / fp64_peak,
+                       "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}
+    return out
 
 
 def run_ours(args):
@@ -562,6 +636,33 @@ def run_ours(args):
     result["rel_l2_vs_c128"] = {"density_max": max(errs_d), "reservoir_max": max(errs_n),
                                 "sample": f"same {len(sample_idx)} instances after {SOLVE_STEPS} steps"}
 
+    # ---- the single-solve configurations: plain complex128 config 0 (1-D) and config 1 (2-D), and
+    # the precision form on config 2, each against its FP64 reference
+    if not args.no_configs:
+        threads = os.cpu_count() or 1
+        fp64_peak = measured_fp64_peak(dev)
+        s0, st0 = workloads.plain_1d()
+        result["plain_config0"] = dict(plain_config_leg(s0, st0, dev, fp64_peak, threads),
+                                       config="1-D radial 1000 nodes on [0,40], order 5, dt 1e-4, 10 000 steps, "
+                                              "complex128")
+        s1, st1 = workloads.plain_2d()
+        result["plain_config1"] = dict(plain_config_leg(s1, st1, dev, fp64_peak, threads),
+                                       config="2-D 256^2 on [-20,20]^2, ring pump, order 3, dt 5e-5, 20 000 steps, "
+                                              "complex128")
+        from nls_gb300 import precision
+        s2, st2 = workloads.precision_2d()
+        res = precision.run(s2, steps=st2, log_every=500, device=local)
+        result["precision_config2"] = {
+            "config": "2-D 1024^2 on [-40,40]^2, ring radius 15 width 2, order 5, dt 1e-5, 50 000 steps; complex64 "
+                      "state, FP64 norm and chemical potential every 500 steps, simulated time in FP64",
+            "c64_node_steps_per_s": res["c64_node_steps_per_s"], "c64_seconds": res["c64_seconds"],
+            "c128_node_steps_per_s": res["c128_node_steps_per_s"], "c128_seconds": res["c128_seconds"],
+            "rel_l2_density": res["rel_l2_density"], "rel_l2_reservoir": res["rel_l2_reservoir"],
+            "reference": "the plain complex128 GPU path on the same problem (pinned to the FP64 oracle at <= 1e-10 "
+                         "by the test suite; the FP64 CPU oracle would need hours for 5e10 node-steps)",
+            "log_entries": len(res["log"])}
+        del res
+
     # ---- served stream (continuous batching) p50/p99
     if args.serve > 0:
         from nls_gb300.serve import Pool, serve
@@ -572,9 +673,14 @@ def run_ours(args):
         pool = Pool(dtype=np.complex64, budget_bytes=80 << 30, chunk_steps=500, device=local)
         st = serve(reqs, rate=200.0, pool=pool)
         pool.close()
+        offered = sum(float(sp.nodes) * k for sp, k in reqs) / float(
+            np.cumsum(np.random.default_rng(7).exponential(1.0 / 200.0, size=len(reqs)))[-1])
         result["serve"] = {"requests": args.serve, "rate_per_s": 200.0, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-                           "node_steps_per_s": st["node_steps_per_s"], "wall_s": st["wall_s"],
-                           "budget_gb": 80, "chunk_steps": 500}
+                           "queue_p50_ms": st["queue_p50_ms"], "queue_p99_ms": st["queue_p99_ms"],
+                           "node_steps_per_s": st["node_steps_per_s"], "offered_node_steps_per_s": offered,
+                           "gpu_busy_frac": st["gpu_busy_frac"], "wall_s": st["wall_s"],
+                           "budget_gb": 80, "chunk_steps": 500,
+                           "stream": "Poisson arrivals (seed 7), steps U[1000, 20000], mixed 1-D/2-D sizes, complex64"}
 
     # ---- CPU oracle on the host cores (bounded sample)
     if not args.no_cpu:
@@ -596,7 +702,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--serve", type=int, default=400, help="requests in the served stream (0 = skip)")
+    ap.add_argument("--serve", type=int, default=10000, help="requests in the served stream (0 = skip)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the plain config 0/1 and precision config 2 legs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
     ap.add_argument("--quick", action="store_true",
                     help="timed batched solves only (no roofline, accuracy, e2e, serve or CPU legs)")

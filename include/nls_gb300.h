@@ -172,18 +172,36 @@ int nls_batch_destroy(nls_batch* batch);
  * set of solves.  budget_bytes bounds the device memory of admitted states and pumps. */
 int nls_pool_create(nls_ctx* ctx, int dtype, size_t budget_bytes, int max_slots, int chunk_steps,
                     nls_pool** out);
-/* Admit one request (host buffers are copied before return).  NLS_ERR_BUSY if no slot or budget
- * is free now; the caller keeps it queued and retries after nls_pool_step. */
+/* Admit one request.  Its pump and initial state are uploaded from the host buffers on the pool's
+ * own copy stream (the buffers may be reused when the call returns); no chunk in flight is waited
+ * for, and the next chunk waits for the upload.  NLS_ERR_BUSY if no slot or budget is free now;
+ * the caller keeps it queued and retries after a chunk completes. */
 int nls_pool_admit(nls_pool* pool, const nls_problem* problem, const void* pumping,
                    const void* u0, int64_t steps, int64_t tag, int* slot);
-/* Advance every admitted request by up to chunk_steps RK4 steps (each stops at its own count).
- * Blocks until the chunk is done; *finished = requests that completed in this chunk. */
+/* Pipelined operation (no reference counterpart: schedulr's workers run one solve at a time).
+ * nls_pool_launch enqueues the next chunk -- every admitted request with steps not yet enqueued
+ * advances by up to chunk_steps RK4 steps, each stopping at its own count -- on the context's
+ * stream and returns at once (*launched = 1), or does nothing (*launched = 0) when two chunks are
+ * already in flight or no request has steps left to enqueue.  nls_pool_wait blocks until the
+ * oldest chunk in flight completes (the pool's lock is released meanwhile, so admissions and
+ * takes proceed) and reports the requests it finished; with no chunk in flight it returns at
+ * once.  nls_pool_ready tells whether the oldest chunk in flight has completed (1 when none is in
+ * flight).  Requests finished by a completed chunk are taken while the next chunk runs. */
+int nls_pool_launch(nls_pool* pool, int* launched);
+int nls_pool_wait(nls_pool* pool, int* finished);
+int nls_pool_ready(nls_pool* pool, int* ready);
+/* Launch (if fewer than two chunks are in flight) and wait for the oldest chunk:
+ * *finished = requests that completed in it. */
 int nls_pool_step(nls_pool* pool, int* finished);
-/* Take one finished request: its tag and final state (host buffer of its size); frees its slot
- * and budget.  NLS_ERR_NOT_READY if none is finished. */
+/* Take one finished request: its tag and final state (host buffer of its size), copied on the
+ * pool's copy stream without waiting for chunks in flight; frees its slot and budget.
+ * NLS_ERR_NOT_READY if none is finished. */
 int nls_pool_take(nls_pool* pool, int64_t* tag, void* u, size_t u_bytes);
 /* Admitted-but-unfinished requests, bytes of budget in use. */
 int nls_pool_status(nls_pool* pool, int* active, size_t* bytes_in_use);
+/* Chunks in flight and the device time of every completed chunk so far (ms, CUDA events on the
+ * context's stream): the pool's GPU-busy time. */
+int nls_pool_info(nls_pool* pool, int* in_flight, double* busy_ms);
 int nls_pool_destroy(nls_pool* pool);
 
 /* ---- allocation-free 2-D solve ------------------------------------------------------------ */

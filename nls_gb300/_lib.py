@@ -91,6 +91,10 @@ SIGNATURES = {
     "nls_pool_create": (_i, [_p, _i, _sz, _i, _i, ctypes.POINTER(_p)]),
     "nls_pool_admit": (_i, [_p, _pp, _p, _p, _i64, _i64, _pi]),
     "nls_pool_step": (_i, [_p, _pi]),
+    "nls_pool_launch": (_i, [_p, _pi]),
+    "nls_pool_wait": (_i, [_p, _pi]),
+    "nls_pool_ready": (_i, [_p, _pi]),
+    "nls_pool_info": (_i, [_p, _pi, _pd]),
     "nls_pool_take": (_i, [_p, _pi64, _p, _sz]),
     "nls_pool_status": (_i, [_p, _pi, _psz]),
     "nls_pool_destroy": (_i, [_p]),

@@ -39,7 +39,15 @@ class Spec:
 
 
 class BatchSolver:
-    def __init__(self, specs, dtype=np.complex64, device: int = 0):
+    """keep_inputs: keep host copies of every instance's pump and initial state as the caller
+    gave them (before the conversion to the working precision) and count the steps run since, so
+    ``accuracy`` can report each result against a complex128 companion solve."""
+
+    def __init__(self, specs, dtype=np.complex64, device: int = 0, keep_inputs: bool = False):
+        self.device = device
+        self.keep_inputs = keep_inputs
+        self._inputs = {}
+        self._steps = [0] * len(specs)
         self.code = _lib.dtype_code(dtype)
         self.ctype, self.rtype = _lib.np_types(self.code)
         self.ctx = _lib.default_context(device)
@@ -63,14 +71,40 @@ class BatchSolver:
             raise ValueError(f"instance {i}: expected {s.nodes} values, got {a.size}")
         return np.asfortranarray(a, dtype=dt) if s.dim == 2 else np.ascontiguousarray(a, dtype=dt)
 
+    def _record(self, i, pumping, u0):
+        self._steps[i] = 0
+        if self.keep_inputs:
+            self._inputs[i] = (np.array(pumping, dtype=np.float64), np.array(u0, dtype=np.complex128))
+
     def set(self, i: int, pumping, u0):
         P = self._field(i, pumping, self.rtype)
         U = self._field(i, u0, self.ctype)
         _lib.check(_lib.lib().nls_batch_set(self.handle, i, _lib.ptr(P), _lib.ptr(U)), "nls_batch_set",
                    self.ctx.handle)
+        self._record(i, pumping, u0)
 
     def run(self, steps: int):
         _lib.check(_lib.lib().nls_batch_run(self.handle, int(steps)), "nls_batch_run", self.ctx.handle)
+        self._steps = [k + int(steps) for k in self._steps]
+
+    def accuracy(self, indices=None):
+        """Per-result relative L2 errors (|psi|^2, reservoir n) of the listed instances (all by
+        default) against complex128 companion solves from their last uploaded inputs (as given,
+        before the conversion to the working precision) over the steps run since, reduced in FP64
+        on the device.  Needs keep_inputs=True."""
+        from dataclasses import replace
+
+        from . import device as ndev
+        if not self.keep_inputs:
+            raise ValueError("accuracy() needs BatchSolver(..., keep_inputs=True)")
+        self.synchronize()
+        out = []
+        for i in (range(len(self.specs)) if indices is None else indices):
+            P, U = self._inputs[i]
+            spec = replace(self.specs[i], pumping=P, u0=U)
+            u_ptr, _ = self.state_pointer(i)
+            out.append(ndev.companion_errors(u_ptr, spec, self._steps[i], self.device))
+        return out
 
     def synchronize(self):
         self.ctx.synchronize()
@@ -103,6 +137,8 @@ class BatchSolver:
         pu = (ctypes.c_void_p * max(count, 1))(*[a.ctypes.data for a in Us])
         _lib.check(_lib.lib().nls_batch_set_many(self.handle, first, count, pp, pu), "nls_batch_set_many",
                    self.ctx.handle)
+        for k in range(count):
+            self._record(first + k, pumpings[k], u0s[k])
 
     def get_many(self, outs=None, first: int = 0, count: int = None):
         """``get`` for instances first, first+1, ... in one call (one wait).  ``outs``: arrays as
@@ -165,6 +201,8 @@ class BatchSolver:
         U = self._block(state_block, sb, "state block")
         _lib.check(_lib.lib().nls_batch_set_packed(self.handle, _lib.ptr(P), _lib.ptr(U)), "nls_batch_set_packed",
                    self.ctx.handle)
+        for i, (p, u) in enumerate(zip(self.packed_views(P, "pump"), self.packed_views(U, "state"))):
+            self._record(i, p, u)
 
     def get_packed(self, out: np.ndarray = None) -> np.ndarray:
         """Every current state into one packed block (``layout``; a new one if ``out`` is None)."""

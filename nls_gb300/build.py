@@ -69,14 +69,22 @@ def _compile(src: str, extra) -> str:
 
 
 def build(verbose_ptxas: bool = False, force: bool = False) -> str:
-    """Compile every translation unit (in parallel) and link libnls_gb300.so; returns its path."""
+    """Compile every translation unit (in parallel) and link libnls_gb300.so; returns its path.
+
+    NLS_GB300_NVCC_FLAGS (whitespace-separated) adds compiler flags, e.g. a -D of a kernel tuning
+    macro; a change of the flags forces a rebuild."""
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    if force:
+    flags = os.environ.get("NLS_GB300_NVCC_FLAGS", "").split()
+    stamp = os.path.join(BUILD, "flags.txt")
+    old = open(stamp).read() if os.path.exists(stamp) else ""
+    if force or old != " ".join(flags):
         for s in SOURCES:
             if os.path.exists(_obj(s)):
                 os.remove(_obj(s))
-    extra = ["-Xptxas", "-v"] if verbose_ptxas else []
+        with open(stamp, "w") as f:
+            f.write(" ".join(flags))
+    extra = (["-Xptxas", "-v"] if verbose_ptxas else []) + flags
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
     if _stale(LIB, objs):

@@ -658,10 +658,10 @@ cudaError_t tile_tx_extra_set(unsigned bytes) {
 
 // ---- streaming step (complex64): occupancy, launch, work items
 
-template <int K>
+template <int K, bool EVEN>
 static int occ_s() {
   typedef StreamCfg<K> G;
-  auto kern = rk4_2d_stream<K>;
+  auto kern = rk4_2d_stream<K, EVEN>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM) != cudaSuccess)
     return 0;
   int nb = 0;
@@ -669,15 +669,32 @@ static int occ_s() {
   return nb;
 }
 
-int stream_2d_blocks_per_sm(int K) { return K == 1 ? occ_s<1>() : (K == 2 ? occ_s<2>() : 0); }
+int stream_2d_blocks_per_sm(int K) {
+  if (K == 1) return std::min(occ_s<1, true>(), occ_s<1, false>());
+  if (K == 2) return std::min(occ_s<2, true>(), occ_s<2, false>());
+  return 0;
+}
 int stream_2d_warps_per_block() { return StreamCfg<1>::WARPS; }
 
-cudaError_t launch_2d_stream(int K, const Inst2D* d_insts, const StripItem* d_items, int n_items, int j_step,
-                             int grid, unsigned* counter, cudaStream_t s) {
-  if (n_items <= 0) return cudaSuccess;
+int stream_kind(int n, const void* u0, const void* u1, const void* P) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(u0) | reinterpret_cast<uintptr_t>(u1) | reinterpret_cast<uintptr_t>(P);
+  return (n % 2 == 0 && (a & 15) == 0) ? STREAM_EVEN : STREAM_ODD;
+}
+
+template <int K>
+static void launch_s(int kinds, const Inst2D* d_insts, const StripItem* d_items, int n_items, int j_step, int grid,
+                     unsigned* counter, cudaStream_t s) {
+  typedef StreamCfg<K> G;
+  if (kinds & STREAM_EVEN) rk4_2d_stream<K, true><<<grid, G::NT, G::SMEM, s>>>(d_insts, d_items, n_items, j_step, counter);
+  if (kinds & STREAM_ODD) rk4_2d_stream<K, false><<<grid, G::NT, G::SMEM, s>>>(d_insts, d_items, n_items, j_step, counter);
+}
+
+cudaError_t launch_2d_stream(int K, int kinds, const Inst2D* d_insts, const StripItem* d_items, int n_items,
+                             int j_step, int grid, unsigned* counter, cudaStream_t s) {
+  if (n_items <= 0 || !(kinds & (STREAM_EVEN | STREAM_ODD))) return cudaSuccess;
   if (!counter || grid <= 0) return cudaErrorInvalidValue;
-  if (K == 1) rk4_2d_stream<1><<<grid, StreamCfg<1>::NT, StreamCfg<1>::SMEM, s>>>(d_insts, d_items, n_items, j_step, counter);
-  else if (K == 2) rk4_2d_stream<2><<<grid, StreamCfg<2>::NT, StreamCfg<2>::SMEM, s>>>(d_insts, d_items, n_items, j_step, counter);
+  if (K == 1) launch_s<1>(kinds, d_insts, d_items, n_items, j_step, grid, counter, s);
+  else if (K == 2) launch_s<2>(kinds, d_insts, d_items, n_items, j_step, grid, counter, s);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }

@@ -122,8 +122,20 @@ struct StreamWin {
   float2 t2X[W], t2Y[W], t3X[W], t3Y[W], t4X[W], t4Y[W];
 };
 
-template <int K>
-__global__ void __launch_bounds__(StreamCfg<K>::NT, K == 1 ? 3 : 2)
+// EVEN: the instance's side is even and its buffers are 16-byte aligned, so a lane's node pair
+// moves as one 16-byte copy (state) and one 8-byte copy (pump) and is stored as one 16-byte store;
+// otherwise every node moves on its own.  Items of the other kind are skipped (the runtime
+// launches both instantiations over the same item list when a group mixes them).
+// CTAs per SM the register budget is sized for (order 3: 3 x 4 warps; order 5: 2 x 4 warps).
+#ifndef NLSG_STREAM_MINB_K1
+#define NLSG_STREAM_MINB_K1 3
+#endif
+#ifndef NLSG_STREAM_MINB_K2
+#define NLSG_STREAM_MINB_K2 2
+#endif
+
+template <int K, bool EVEN>
+__global__ void __launch_bounds__(StreamCfg<K>::NT, K == 1 ? NLSG_STREAM_MINB_K1 : NLSG_STREAM_MINB_K2)
 rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ items, int n_items, int j_step,
               unsigned* __restrict__ counter) {
   typedef StreamCfg<K> G;
@@ -151,8 +163,17 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
     const bool even = !(n & 1) &&
                       ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst) |
                         reinterpret_cast<uintptr_t>(Pg)) & 15) == 0;
+    if (even != EVEN) continue;
     const int x = (int)it.x0 + 2 * lane;
     const bool in0 = x < n, in1 = x + 1 < n;
+    // per-lane column offsets clamped into the grid (a lane beyond it copies zero bytes from
+    // column 0) and the byte counts of its copies
+    const float2* __restrict__ src0 = src + (in0 ? x : 0);
+    const float2* __restrict__ src1 = src + (in1 ? x + 1 : 0);
+    const float* __restrict__ P0 = Pg + (in0 ? x : 0);
+    const float* __restrict__ P1 = Pg + (in1 ? x + 1 : 0);
+    const uint32_t szu0 = EVEN ? (in0 ? 16u : 0u) : (in0 ? 8u : 0u), szu1 = in1 ? 8u : 0u;
+    const uint32_t szp0 = EVEN ? (in0 ? 8u : 0u) : (in0 ? 4u : 0u), szp1 = in1 ? 4u : 0u;
     const bool out0 = in0 && x >= (int)it.ox0 && x < (int)it.ox1;
     const bool out1 = in1 && x + 1 >= (int)it.ox0 && x + 1 < (int)it.ox1;
     const int y0 = it.y0, y1 = it.y1;
@@ -185,24 +206,24 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
     const int ib = y0 - 4 * K > 0 ? y0 - 4 * K : 0;   // first row loaded
     const int ie = y1 + 4 * K;                        // one past the last iteration
     // iterations whose load row and four stage rows all lie inside the grid and inside the rows
-    // this segment needs: no per-stage checks
-    const int clean_lo = y0 + 4 * K, clean_hi = n < ie ? n : ie;
+    // this segment needs, and whose prefetch row lies inside the grid and the segment: no checks
+    const int clean_lo = y0 + 4 * K, clean_hi = (n < ie ? n : ie) - D;
 
-    // cp.async of row `row` into its ring slot (zero-filled where the row or a node lies outside
-    // the grid); every lane copies its own node pair
-    auto issue_row = [&](int row) {
+    // cp.async of row `row` into its ring slot; every lane copies its own node pair.  FULL: the
+    // row is known to lie inside the grid; otherwise rows beyond it arrive zero-filled.
+    auto issue_row = [&](int row, auto FULLc) {
+      constexpr bool FULL = decltype(FULLc)::value;
       const uint32_t slot = ring + (uint32_t)((row & (R - 1)) * G::ROWB);
-      const bool rin = row < n;
-      const size_t q = (size_t)(rin ? row : 0) * n + (in0 ? x : 0);
-      if (even) {
-        cp_async_sz<16>(slot + lane * 16, src + q, rin && in0 ? 16u : 0u);
-        cp_async_sz<8>(slot + 512 + lane * 8, Pg + q, rin && in0 ? 8u : 0u);
+      const bool rin = FULL || row < n;
+      const size_t q = (size_t)(rin ? row : 0) * n;
+      if (EVEN) {
+        cp_async_sz<16>(slot + lane * 16, src0 + q, rin ? szu0 : 0u);
+        cp_async_sz<8>(slot + 512 + lane * 8, P0 + q, rin ? szp0 : 0u);
       } else {
-        const size_t q1 = (size_t)(rin ? row : 0) * n + (in1 ? x + 1 : 0);
-        cp_async_sz<8>(slot + lane * 16, src + q, rin && in0 ? 8u : 0u);
-        cp_async_sz<8>(slot + lane * 16 + 8, src + q1, rin && in1 ? 8u : 0u);
-        cp_async_sz<4>(slot + 512 + lane * 8, Pg + q, rin && in0 ? 4u : 0u);
-        cp_async_sz<4>(slot + 512 + lane * 8 + 4, Pg + q1, rin && in1 ? 4u : 0u);
+        cp_async_sz<8>(slot + lane * 16, src0 + q, rin ? szu0 : 0u);
+        cp_async_sz<8>(slot + lane * 16 + 8, src1 + q, rin ? szu1 : 0u);
+        cp_async_sz<4>(slot + 512 + lane * 8, P0 + q, rin ? szp0 : 0u);
+        cp_async_sz<4>(slot + 512 + lane * 8 + 4, P1 + q, rin ? szp1 : 0u);
       }
     };
 
@@ -215,7 +236,7 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
 
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      if (ib + d < ie) issue_row(ib + d);
+      if (ib + d < ie) issue_row(ib + d, std::false_type{});
       async_commit();
     }
 
@@ -235,7 +256,8 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
         w.uY[P] = f2(v.y, v.w);
         w.pc[P] = mul2(c.c12, p);
       }
-      if (i + D < ie) issue_row(i + D);
+      if (!CHECK) issue_row(i + D, std::true_type{});
+      else if (i + D < ie) issue_row(i + D, std::false_type{});
       async_commit();
 
       // stage 1 at row i - K: input u, output t2 = u + q1, a = q1
@@ -304,7 +326,7 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
           const float2 nX = fma2(c.third, add2(w.aX[C], qX), w.uX[C]);
           const float2 nY = fma2(c.third, add2(w.aY[C], qY), w.uY[C]);
           const size_t q = (size_t)r * n + x;
-          if (even) {
+          if (EVEN) {
             if (out0) *reinterpret_cast<float4*>(dst + q) = make_float4(nX.x, nY.x, nX.y, nY.y);
           } else {
             if (out0) dst[q] = f2(nX.x, nY.x);

@@ -76,10 +76,15 @@ cudaError_t tile_tx_extra_set(unsigned bytes);
 // Streaming step (TILE_STREAM): CTAs per SM (sets the shared-memory attribute; call outside any
 // capture), warps per CTA, and the launch.  counter: two device unsigned ints, zero before the
 // first launch; every launch leaves them zero again.
+// kinds: which kernel forms a launch runs -- STREAM_EVEN (instances with an even side and 16-byte
+// aligned buffers: paired 16-byte copies and stores) and/or STREAM_ODD (per-node copies); each
+// form skips the other kind's items, so a group holding both launches both over one item list.
+enum { STREAM_EVEN = 1, STREAM_ODD = 2 };
+int stream_kind(int n, const void* u0, const void* u1, const void* P);
 int stream_2d_blocks_per_sm(int K);
 int stream_2d_warps_per_block();
-cudaError_t launch_2d_stream(int K, const Inst2D* d_insts, const StripItem* d_items, int n_items, int j_step,
-                             int grid, unsigned* counter, cudaStream_t s);
+cudaError_t launch_2d_stream(int K, int kinds, const Inst2D* d_insts, const StripItem* d_items, int n_items,
+                             int j_step, int grid, unsigned* counter, cudaStream_t s);
 // Strip geometry of an n-wide grid (first strip against the left edge, interior strips with a
 // 4K halo on both sides, last strip against the right edge), the segment height that minimises
 // the estimated makespan of a set of grids over `slots` warps, the items of one instance, and

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <mutex>
 #include <string>
@@ -282,16 +283,18 @@ static int solve_2d_stream(nls_ctx* ctx, const nls_problem* pr, const Stencil2D&
   CK(ctx, cudaMemcpyAsync(dT, items.data(), sizeof(StripItem) * n_items, cudaMemcpyHostToDevice, ctx->stream));
   CK(ctx, cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned), ctx->stream));
   const int grid = stream_grid(ctx, op.K, n_items);
+  const int kinds = stream_kind(n, I.u[0], I.u[1], P);
   const int S = 64;  // even: a replay returns the state to the caller's buffer
   CK(ctx, replay(ctx, iters / S, [&]() -> cudaError_t {
        for (int j = 0; j < S; ++j) {
-         cudaError_t e = launch_2d_stream(op.K, dI, dT, n_items, j, grid, counter, ctx->stream);
+         cudaError_t e = launch_2d_stream(op.K, kinds, dI, dT, n_items, j, grid, counter, ctx->stream);
          if (e) return e;
        }
        return cudaSuccess;
      }));
   const int64_t rem = iters % S;
-  for (int64_t j = 0; j < rem; ++j) CK(ctx, launch_2d_stream(op.K, dI, dT, n_items, (int)j, grid, counter, ctx->stream));
+  for (int64_t j = 0; j < rem; ++j)
+    CK(ctx, launch_2d_stream(op.K, kinds, dI, dT, n_items, (int)j, grid, counter, ctx->stream));
   if (rem & 1) CK(ctx, cudaMemcpyAsync(u, ctx->scratch.p, N * csize(NLS_C64), cudaMemcpyDeviceToDevice, ctx->stream));
   ctx->launches += iters;
   return NLS_OK;
@@ -556,6 +559,7 @@ struct Group2D {
   std::vector<StripItem> sitems_h;
   StripItem* sitems = nullptr;
   unsigned* counter = nullptr;
+  int kinds = 0;           // STREAM_EVEN / STREAM_ODD forms its members need
 };
 
 struct Member {
@@ -710,6 +714,11 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
                                 ctx->stream));
       G.tma = false;
       G.grid = stream_grid(ctx, G.K, std::max(1, G.n_items));
+      G.kinds = 0;
+      for (int i : G.idx) {
+        const Member& M = b->m[i];
+        G.kinds |= stream_kind(M.pr.n, M.u[0], M.u[1], M.P);
+      }
       continue;
     }
     G.items = (TileItem*)(b->mem + g2items[g]);
@@ -804,7 +813,7 @@ static cudaError_t batch_sequence(nls_batch* b, int64_t steps) {
   for (int64_t j = 0; j < steps; ++j) {
     for (auto& G : b->g2)
       if ((e = G.shape == TILE_STREAM
-                   ? launch_2d_stream(G.K, G.d, G.sitems, G.n_items, (int)j, G.grid, G.counter, ctx->stream)
+                   ? launch_2d_stream(G.K, G.kinds, G.d, G.sitems, G.n_items, (int)j, G.grid, G.counter, ctx->stream)
                : G.tma ? launch_2d_fused_tma(G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream,
                                              ctx->wait_flag)
                        : launch_2d_fused(dtype, G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream)))
@@ -854,12 +863,14 @@ static int64_t batch_launches(const nls_batch* b, int64_t steps) {
 struct Slot {
   bool used = false, done = false;
   nls_problem pr;
-  int64_t tag = 0, remaining = 0;
+  int64_t tag = 0;
+  int64_t remaining = 0;        // steps not yet enqueued in a chunk
+  int64_t finish_chunk = -1;    // chunk whose completion finishes the request (all steps enqueued)
   size_t off = 0, bytes = 0;
   size_t N = 0;
   char* u[2] = {nullptr, nullptr};
   char* P = nullptr;
-  int parity = 0;
+  int parity = 0;               // buffer holding the state after every enqueued step
   int kind = 0;       // 1 = 1-D resident, 2 = 2-D fused
   int K = 0, cl = 0, shape = 0, ntiles = 0, tiles_x = 0;
   Stencil1D op1;
@@ -869,6 +880,13 @@ struct Slot {
   std::vector<unsigned char> maps;   // 3 tensor maps (host copy), when tma
 };
 
+// A chunk enqueued on the context's stream: descriptor buffer `buf` (two, so the next chunk's
+// image can be uploaded while the previous chunk runs) and its start/done events.
+struct PoolChunk {
+  int64_t id;
+  int buf;
+};
+
 struct nls_pool {
   nls_ctx* ctx;
   int dtype;
@@ -876,8 +894,16 @@ struct nls_pool {
   Arena arena;
   std::vector<Slot> slots;
   uint64_t seq = 0;
-  DevBuf d_desc;
+  DevBuf d_desc[2];
   std::vector<char> h_desc;
+  cudaStream_t copy = nullptr;          // admission uploads and result downloads
+  cudaEvent_t ev_upload = nullptr;      // recorded after the latest admission upload
+  bool upload_pending = false;          // the next chunk must wait for ev_upload
+  cudaEvent_t ev_start[2] = {}, ev_done[2] = {};
+  std::deque<PoolChunk> inflight;       // at most two, oldest first
+  int64_t next_chunk = 0;
+  double busy_ms = 0.0;                 // device time of the completed chunks
+  bool waiting = false;                 // a thread is blocked in nls_pool_wait
   std::mutex mu;
 };
 
@@ -1328,6 +1354,21 @@ NLS_API int nls_batch_destroy(nls_batch* b) {
 
 // ---- pool
 
+static void pool_release(nls_pool* p) {
+  if (p->copy) cudaStreamSynchronize(p->copy);
+  if (p->ctx->stream) cudaStreamSynchronize(p->ctx->stream);
+  if (p->ctx->aux) cudaStreamSynchronize(p->ctx->aux);
+  for (int b = 0; b < 2; ++b) {
+    p->d_desc[b].release();
+    if (p->ev_start[b]) cudaEventDestroy(p->ev_start[b]);
+    if (p->ev_done[b]) cudaEventDestroy(p->ev_done[b]);
+  }
+  if (p->ev_upload) cudaEventDestroy(p->ev_upload);
+  if (p->copy) cudaStreamDestroy(p->copy);
+  p->arena.destroy();
+  delete p;
+}
+
 NLS_API int nls_pool_create(nls_ctx* ctx, int dtype, size_t budget_bytes, int max_slots, int chunk_steps,
                             nls_pool** out) {
   if (!ctx) return NLS_ERR_INVALID;
@@ -1343,9 +1384,15 @@ NLS_API int nls_pool_create(nls_ctx* ctx, int dtype, size_t budget_bytes, int ma
   p->chunk = chunk_steps;
   p->slots.resize(max_slots);
   cudaError_t e = p->arena.init(budget_bytes);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->copy, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_upload, cudaEventDisableTiming);
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    e = cudaEventCreate(&p->ev_start[b]);
+    if (e == cudaSuccess) e = cudaEventCreate(&p->ev_done[b]);
+  }
   if (e != cudaSuccess) {
-    delete p;
-    return fail_cuda(ctx, e, "pool arena");
+    pool_release(p);
+    return fail_cuda(ctx, e, "pool set-up");
   }
   *out = p;
   return NLS_OK;
@@ -1412,37 +1459,42 @@ NLS_API int nls_pool_admit(nls_pool* p, const nls_problem* problem, const void* 
       S.maps.assign(hm, hm + tma_map_bytes());
     }
   }
-  cudaError_t e1 = cudaMemcpyAsync(S.P, pumping, S.N * rsize(p->dtype), cudaMemcpyHostToDevice, ctx->stream);
-  cudaError_t e2 = cudaMemcpyAsync(S.u[0], u0, S.N * csize(p->dtype), cudaMemcpyHostToDevice, ctx->stream);
-  cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
+  // Upload on the pool's copy stream: the chunks running on the context's stream are not waited
+  // for (the region is free memory that no chunk in flight touches); the next chunk waits for the
+  // upload's event.  Copies from pageable memory return once the bytes are staged.
+  cudaError_t e1 = cudaMemcpyAsync(S.P, pumping, S.N * rsize(p->dtype), cudaMemcpyHostToDevice, p->copy);
+  cudaError_t e2 = cudaMemcpyAsync(S.u[0], u0, S.N * csize(p->dtype), cudaMemcpyHostToDevice, p->copy);
+  cudaError_t e3 = cudaEventRecord(p->ev_upload, p->copy);
   if (e1 || e2 || e3) {
     p->arena.release(S.off, S.bytes);
     return fail_cuda(ctx, e1 ? e1 : (e2 ? e2 : e3), "pool upload");
   }
+  p->upload_pending = true;
   p->slots[free_slot] = S;
   if (slot) *slot = free_slot;
   return NLS_OK;
 }
 
-NLS_API int nls_pool_step(nls_pool* p, int* finished) {
-  if (!p) return NLS_ERR_INVALID;
+// Enqueue the next chunk (every admitted request with steps not yet enqueued advances by up to
+// `chunk` steps) if fewer than two chunks are in flight.  Called with p->mu held.
+static int pool_launch_locked(nls_pool* p, int* launched) {
   nls_ctx* ctx = p->ctx;
-  std::lock_guard<std::mutex> lk(p->mu);
+  *launched = 0;
+  if (p->inflight.size() >= 2) return NLS_OK;
   CK(ctx, cudaSetDevice(ctx->device));
   const int dtype = p->dtype;
-  // group the active slots
   std::map<std::pair<int, int>, std::vector<int>> g1;
   std::map<std::tuple<int, int, int>, std::vector<int>> g2;   // (K, shape, tma)
   int64_t max_steps = 0;
   for (size_t i = 0; i < p->slots.size(); ++i) {
     const Slot& S = p->slots[i];
-    if (!S.used || S.done) continue;
+    if (!S.used || S.done || S.remaining <= 0) continue;
     if (S.kind == 1) g1[{S.K, S.cl}].push_back((int)i);
     else g2[std::make_tuple(S.K, S.shape, S.tma ? 1 : 0)].push_back((int)i);
     max_steps = std::max<int64_t>(max_steps, std::min<int64_t>(S.remaining, p->chunk));
   }
-  if (finished) *finished = 0;
   if (g1.empty() && g2.empty()) return NLS_OK;
+  const int buf = (int)(p->next_chunk & 1);
   // work items of each 2-D group: tiles, or strip items over the group's current mix
   std::vector<std::vector<StripItem>> sitems(g2.size());
   {
@@ -1467,7 +1519,8 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
     size_t gi = 0;
     for (auto& kv : g2) {
       if (std::get<1>(kv.first) == TILE_STREAM) {
-        bytes += align256(sizeof(Inst2D) * kv.second.size()) + align256(sizeof(StripItem) * std::max<size_t>(1, sitems[gi].size())) + 256;
+        bytes += align256(sizeof(Inst2D) * kv.second.size()) +
+                 align256(sizeof(StripItem) * std::max<size_t>(1, sitems[gi].size())) + 256;
       } else {
         int items = 0;
         for (int i : kv.second) items += p->slots[i].ntiles;
@@ -1478,9 +1531,10 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
     }
   }
   p->h_desc.assign(bytes, 0);
-  CK(ctx, p->d_desc.ensure(bytes));
+  CK(ctx, p->d_desc[buf].ensure(bytes));
+  char* d = (char*)p->d_desc[buf].p;
   struct L1 { int K, cl, seg, count; size_t off; };
-  struct L2 { int K, shape, n_items, grid; size_t off, off_items, off_counter; bool tma; };
+  struct L2 { int K, shape, n_items, grid; size_t off, off_items, off_counter; bool tma; int kinds; };
   std::vector<L1> l1;
   std::vector<L2> l2;
   size_t off = 0;
@@ -1513,9 +1567,10 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
                                        : align256(sizeof(TileItem) * items));
     TileItem* it = (TileItem*)(p->h_desc.data() + ioff);
     if (stream && items) std::memcpy(p->h_desc.data() + ioff, sitems[gi].data(), sizeof(StripItem) * items);
-    int q_items = 0;
+    int q_items = 0, kinds = 0;
     for (size_t k = 0; k < kv.second.size(); ++k) {
       const Slot& S = p->slots[kv.second[k]];
+      if (stream) kinds |= stream_kind(S.pr.n, S.u[0], S.u[1], S.P);
       Inst2D& I = h[k];
       I.u[0] = S.u[0]; I.u[1] = S.u[1]; I.P = S.P; I.n = S.pr.n; I.tiles_x = S.tiles_x;
       I.parity = S.parity; I.steps = std::min<int64_t>(S.remaining, p->chunk);
@@ -1523,7 +1578,7 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
       set_params(I);
       if (tma) {
         std::memcpy(p->h_desc.data() + moff + k * tma_map_bytes(), S.maps.data(), tma_map_bytes());
-        I.tmap = (char*)p->d_desc.p + moff + k * tma_map_bytes();
+        I.tmap = d + moff + k * tma_map_bytes();
       }
       if (!stream)
         for (int q = 0; q < S.ntiles; ++q) it[q_items++] = TileItem{(int)k, q};
@@ -1535,12 +1590,18 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
       const int occ = tma ? fused_2d_tma_blocks_per_sm(K, shape) : fused_2d_blocks_per_sm(dtype, K, shape);
       grid = std::max(1, std::min(items, ctx->sm_count * std::max(1, occ)));
     }
-    l2.push_back(L2{K, shape, items, grid, off, ioff, moff, tma});
+    l2.push_back(L2{K, shape, items, grid, off, ioff, moff, tma, kinds});
     off = moff + (stream ? 256 : align256(tma_map_bytes() * kv.second.size()));
     ++gi;
   }
-  char* d = (char*)p->d_desc.p;
+  // The previous user of this descriptor buffer is the chunk before the one in flight, already
+  // complete; the upload is ordered on the context's stream after the chunk in flight.
   CK(ctx, cudaMemcpyAsync(d, p->h_desc.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
+  if (p->upload_pending) {
+    CK(ctx, cudaStreamWaitEvent(ctx->stream, p->ev_upload, 0));
+    p->upload_pending = false;
+  }
+  CK(ctx, cudaEventRecord(p->ev_start[buf], ctx->stream));
   if (!l1.empty()) {
     CK(ctx, cudaEventRecord(ctx->ev_fork, ctx->stream));
     CK(ctx, cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0));
@@ -1553,7 +1614,7 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
     for (auto& L : l2) {
       const Inst2D* dI = (const Inst2D*)(d + L.off);
       if (L.shape == TILE_STREAM) {
-        CK(ctx, launch_2d_stream(L.K, dI, (const StripItem*)(d + L.off_items), L.n_items, (int)j, L.grid,
+        CK(ctx, launch_2d_stream(L.K, L.kinds, dI, (const StripItem*)(d + L.off_items), L.n_items, (int)j, L.grid,
                                  (unsigned*)(d + L.off_counter), ctx->stream));
       } else {
         const TileItem* dT = (const TileItem*)(d + L.off_items);
@@ -1567,25 +1628,87 @@ NLS_API int nls_pool_step(nls_pool* p, int* finished) {
     CK(ctx, cudaEventRecord(ctx->ev_join, ctx->aux));
     CK(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
   }
-  CK(ctx, cudaStreamSynchronize(ctx->stream));
-  {
-    int st = check_timeout(ctx);
-    if (st) return st;
-  }
-  int done = 0;
+  CK(ctx, cudaEventRecord(p->ev_done[buf], ctx->stream));
+  const int64_t id = p->next_chunk++;
   for (auto& S : p->slots) {
-    if (!S.used || S.done) continue;
+    if (!S.used || S.done || S.remaining <= 0) continue;
     const int64_t st = std::min<int64_t>(S.remaining, p->chunk);
     S.remaining -= st;
     if (S.kind == 2) S.parity ^= (int)(st & 1);
-    if (S.remaining == 0) {
-      S.done = true;
-      S.finish_seq = ++p->seq;
-      ++done;
-    }
+    if (S.remaining == 0) S.finish_chunk = id;
+  }
+  p->inflight.push_back(PoolChunk{id, buf});
+  *launched = 1;
+  return NLS_OK;
+}
+
+NLS_API int nls_pool_launch(nls_pool* p, int* launched) {
+  if (!p) return NLS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(p->mu);
+  int l = 0;
+  int st = pool_launch_locked(p, &l);
+  if (launched) *launched = l;
+  return st;
+}
+
+NLS_API int nls_pool_wait(nls_pool* p, int* finished) {
+  if (!p) return NLS_ERR_INVALID;
+  nls_ctx* ctx = p->ctx;
+  std::unique_lock<std::mutex> lk(p->mu);
+  if (finished) *finished = 0;
+  if (p->inflight.empty()) return NLS_OK;
+  if (p->waiting) return fail(ctx, NLS_ERR_BUSY, "another thread is waiting on this pool");
+  const PoolChunk c = p->inflight.front();
+  p->waiting = true;
+  lk.unlock();           // admissions, takes and the next launch proceed while the chunk runs
+  cudaError_t e = cudaEventSynchronize(p->ev_done[c.buf]);
+  lk.lock();
+  p->waiting = false;
+  if (e != cudaSuccess) return fail_cuda(ctx, e, "waiting for a pool chunk");
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, p->ev_start[c.buf], p->ev_done[c.buf]) == cudaSuccess) p->busy_ms += ms;
+  p->inflight.pop_front();
+  int done = 0;
+  for (auto& S : p->slots) {
+    if (!S.used || S.done || S.finish_chunk != c.id) continue;
+    S.done = true;
+    S.finish_seq = ++p->seq;
+    ++done;
   }
   if (finished) *finished = done;
+  if (p->inflight.empty()) {
+    int st = check_timeout(ctx);   // nothing in flight: reading the status word waits for nothing
+    if (st) return st;
+  }
   return NLS_OK;
+}
+
+NLS_API int nls_pool_ready(nls_pool* p, int* ready) {
+  if (!p || !ready) return NLS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (p->inflight.empty()) {
+    *ready = 1;
+    return NLS_OK;
+  }
+  const cudaError_t e = cudaEventQuery(p->ev_done[p->inflight.front().buf]);
+  if (e == cudaErrorNotReady) {
+    *ready = 0;
+    return NLS_OK;
+  }
+  if (e != cudaSuccess) return fail_cuda(p->ctx, e, "querying a pool chunk");
+  *ready = 1;
+  return NLS_OK;
+}
+
+NLS_API int nls_pool_step(nls_pool* p, int* finished) {
+  if (!p) return NLS_ERR_INVALID;
+  {
+    std::lock_guard<std::mutex> lk(p->mu);
+    int l = 0;
+    int st = pool_launch_locked(p, &l);
+    if (st) return st;
+  }
+  return nls_pool_wait(p, finished);
 }
 
 NLS_API int nls_pool_take(nls_pool* p, int64_t* tag, void* u, size_t u_bytes) {
@@ -1603,8 +1726,10 @@ NLS_API int nls_pool_take(nls_pool* p, int64_t* tag, void* u, size_t u_bytes) {
   if (u) {
     if (u_bytes < need) return fail(ctx, NLS_ERR_INVALID, "output buffer too small");
     CK(ctx, cudaSetDevice(ctx->device));
-    CK(ctx, cudaMemcpyAsync(u, S.u[S.parity], need, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    // the state is final (its last chunk completed); the copy stream does not wait for the
+    // chunks still running on the context's stream
+    CK(ctx, cudaMemcpyAsync(u, S.u[S.parity], need, cudaMemcpyDeviceToHost, p->copy));
+    CK(ctx, cudaStreamSynchronize(p->copy));
   }
   if (tag) *tag = S.tag;
   p->arena.release(S.off, S.bytes);
@@ -1622,13 +1747,17 @@ NLS_API int nls_pool_status(nls_pool* p, int* active, size_t* bytes_in_use) {
   return NLS_OK;
 }
 
+NLS_API int nls_pool_info(nls_pool* p, int* in_flight, double* busy_ms) {
+  if (!p) return NLS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (in_flight) *in_flight = (int)p->inflight.size();
+  if (busy_ms) *busy_ms = p->busy_ms;
+  return NLS_OK;
+}
+
 NLS_API int nls_pool_destroy(nls_pool* p) {
   if (!p) return NLS_ERR_INVALID;
   cudaSetDevice(p->ctx->device);
-  cudaStreamSynchronize(p->ctx->stream);
-  cudaStreamSynchronize(p->ctx->aux);
-  p->d_desc.release();
-  p->arena.destroy();
-  delete p;
+  pool_release(p);
   return NLS_OK;
 }

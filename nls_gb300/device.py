@@ -137,3 +137,38 @@ def density_errors(u: torch.Tensor, u_ref: torch.Tensor, P64: torch.Tensor, coef
 def launches(device: int = 0) -> int:
     """Kernel launches issued so far by this process's context on the device."""
     return context(device).launches
+
+
+def companion_errors(state, spec, steps: int, device: int = 0):
+    """Relative L2 errors of |psi|^2 and of the reservoir n of a result against a complex128
+    companion solve of the same problem (the plain path, pinned to the FP64 oracle) from the
+    spec's pump and initial state over the same number of steps, reduced in FP64 on the device.
+
+    ``state`` is the result as a host array (the spec's shape; Fortran order in 2-D, as the batch
+    and pool return it) or a raw device pointer to a complex64 result in that memory order."""
+    dev = torch.device("cuda", device)
+    shape = (spec.n, spec.n) if spec.dim == 2 else (spec.n,)
+    order = "F" if spec.dim == 2 else "C"
+    u64 = torch.tensor(np.ravel(np.asarray(spec.u0, dtype=np.complex128), order=order).copy(),
+                       device=dev).reshape(shape)
+    P64 = torch.tensor(np.ravel(np.asarray(spec.pumping, dtype=np.float64), order=order).copy(),
+                       device=dev).reshape(shape)
+    solve_(u64, P64, order=spec.order, dt=spec.dt, dx=spec.dx, coeffs=spec.coeffs, iters=int(steps))
+    if isinstance(state, np.ndarray):
+        code = _lib.dtype_code(state.dtype)
+        ct = torch.complex64 if code == _lib.NLS_C64 else torch.complex128
+        t = torch.tensor(np.ravel(state, order=order).copy(), dtype=ct, device=dev)
+        ptr = t.data_ptr()
+    else:
+        code, t, ptr = _lib.NLS_C64, None, int(state)
+    c = np.asarray(spec.coeffs, dtype=np.float64)
+    ctx = context(device)
+    ext = _ext_stream(ctx)
+    ext.wait_stream(torch.cuda.current_stream(dev))
+    d, r = ctypes.c_double(), ctypes.c_double()
+    st = _lib.lib().nls_density_error_device(ctx.handle, code, spec.nodes, ctypes.c_void_p(ptr),
+                                             ctypes.c_void_p(u64.data_ptr()), ctypes.c_void_p(P64.data_ptr()),
+                                             float(c[11]), float(c[12]), float(c[13]), ctypes.byref(d),
+                                             ctypes.byref(r))
+    _lib.check(st, "nls_density_error_device", ctx.handle)
+    return d.value, r.value

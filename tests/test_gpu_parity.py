@@ -475,3 +475,83 @@ def test_2d_c64_stream_large_grids(gpu, oracle_lib, order, n):
                               threads=os.cpu_count() or 1)
     got = _device_solve(gpu, s, iters, np.complex64, 15)
     assert rel(got, want32) <= 3e-5
+
+
+def test_pipelined_serving_matches_single_solves(gpu):
+    """serve(): two chunks in flight, admissions on the copy stream while chunks run, takes while
+    the next chunk runs -- every request's result equals its single solve bit for bit."""
+    from nls_gb300 import workloads as w
+    from nls_gb300.serve import Pool, serve
+    reqs = []
+    for i in range(14):
+        spec = w.mix_instance(300 + i, 1 + (i % 2), variant=15 if i % 4 == 1 else -1)
+        reqs.append((spec, 30 + 17 * i))
+    pool = Pool(budget_bytes=1 << 30, chunk_steps=25)
+    st = serve(reqs, rate=400.0, pool=pool, keep_results=True)
+    assert len(st["results"]) == len(reqs)
+    assert 0.0 < st["gpu_busy_frac"] <= 1.0 and np.isfinite(st["queue_p99_ms"])
+    for tag, (spec, steps) in enumerate(reqs):
+        want = _device_solve(gpu, spec, steps, np.complex64, spec.variant)
+        got = st["results"][tag]
+        assert np.array_equal(got, want.astype(got.dtype)), tag
+    pool.close()
+
+
+def test_pool_launch_wait_protocol(gpu):
+    """Two chunks in flight at most; wait() completes the oldest; requests taken while a chunk runs."""
+    from nls_gb300 import workloads as w
+    from nls_gb300.serve import Pool
+    pool = Pool(budget_bytes=1 << 30, chunk_steps=10)
+    a, b = w.mix_instance(7, 2), w.mix_instance(8, 1)
+    pool.admit(a, 10, 0)
+    pool.admit(b, 35, 1)
+    assert pool.launch() and pool.launch() and not pool.launch()
+    assert pool.info()[0] == 2
+    assert pool.wait() == 1                      # the first chunk finishes request 0
+    got = pool.take_with_state()                 # taken while the second chunk runs
+    assert got is not None and got[0] == 0
+    assert pool.launch()                         # steps 20..30 of request 1
+    while pool.info()[0]:
+        pool.wait()
+    assert pool.launch() and pool.wait() == 1    # steps 30..35
+    got1 = pool.take_with_state()
+    assert got1[0] == 1
+    assert np.array_equal(got[1], _device_solve(gpu, a, 10, np.complex64, -1))
+    assert np.array_equal(got1[1], _device_solve(gpu, b, 35, np.complex64, -1))
+    assert not pool.launch() and pool.wait() == 0 and pool.ready()
+    pool.close()
+
+
+def test_per_result_accuracy_of_batch_and_pool(gpu):
+    """Opt-in per-result relative L2 of |psi|^2 and n against complex128 companion solves: the
+    batch's figures equal a direct computation, and the batch's and the pool's meet the precision
+    form's 1e-4."""
+    from nls_gb300 import workloads as w
+    from nls_gb300.batch import BatchSolver
+    from nls_gb300.serve import Pool
+    specs = [w.mix_instance(40 + i, 1 + (i % 2)) for i in range(4)]
+    b = BatchSolver(specs, dtype=np.complex64, keep_inputs=True)
+    b.run(60)
+    b.run(40)
+    acc = b.accuracy()
+    for i, s in enumerate(specs):
+        got = b.get(i)
+        d, r = acc[i]
+        assert 0.0 < d <= 1e-4 and 0.0 <= r <= 1e-4, (i, d, r)
+        u64 = _device_solve(gpu, s, 100, np.complex128, -1)
+        dd = rel(np.abs(got.astype(np.complex128)) ** 2, np.abs(u64) ** 2)
+        assert abs(dd - d) <= 1e-6 * dd, (i, dd, d)
+    pool = Pool(budget_bytes=1 << 30, chunk_steps=30, keep_inputs=True)
+    for i, s in enumerate(specs):
+        pool.admit(s, 50 + 10 * i, i)
+    seen = 0
+    while seen < len(specs):
+        pool.step()
+        while True:
+            got = pool.take_with_accuracy()
+            if got is None:
+                break
+            tag, state, (d, r) = got
+            assert 0.0 < d <= 1e-4 and r <= 1e-4, (tag, d, r)
+            seen += 1
+    pool.close()
