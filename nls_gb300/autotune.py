@@ -8,7 +8,8 @@ variants on a seeded instance of that size and keeps the fastest:
   128x32 / 512 (2), 32x32 / 256 (3), 64x64 / 1024 (4), 128x32 / 1024 (5), 64x(64+8K) / 512 (6) or
   768/640 (7), or register-resident row-strip tiles (rk4_2d_reg, complex64) with region 64x80 /
   512 (8), 64x96 / 384 (9), 64x96 / 256 (10), 64x64 / 512 (11), 64x72 / 256 (12), 64x72 / 384 (13)
-  or 64x80 / 256 (14);
+  or 64x80 / 256 (14), or the streaming wavefront over 64-column strips (rk4_2d_stream, complex64,
+  15);
 * 1-D: the resident kernel on 1, 2, 4, 8 or 16 CTAs of a cluster, or 0 = unfused stage kernels.
 
 Two objectives: ``mode="single"`` times one solve of the size (latency of a lone solve), and
@@ -51,7 +52,7 @@ def bucket(n: int) -> int:
 def candidates(dim: int, dtype, n: int):
     c64 = np.dtype(dtype) == np.dtype(np.complex64)
     if dim == 2:
-        return [10, 12, 13, 14, 9, 8, 11, 6, 1, 7, 2, 3, 4, 5, 0] if c64 else [0, 3]
+        return [15, 10, 12, 13, 14, 9, 8, 11, 6, 1, 7, 2, 3, 4, 5, 0] if c64 else [0, 3]
     out = []
     lim = 4096 if c64 else 2048
     for cl in (1, 2, 4, 8, 16):
