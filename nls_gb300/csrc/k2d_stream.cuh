@@ -47,14 +47,17 @@ struct StaticFor<E, E> {
 template <int K>
 struct StreamCfg {
   static constexpr int H = 4 * K;          // horizontal halo of a strip edge inside the grid
-  static constexpr int W = 4 * K + 1;      // rows held per window (rows i-4K .. i)
-  static constexpr int D = 4;              // rows prefetched ahead of the one being consumed
-  static constexpr int R = 8;              // ring slots per warp (R >= D + 2, a power of two)
+  // The loop is unrolled by W iterations; W is also the number of rows each window holds (at
+  // least 4K + 1) and the depth of the shared-memory row ring, so the ring slot of row i is the
+  // unroll phase (i - first row) mod W, a compile-time constant, and so is every slot offset.
+  static constexpr int W = K == 1 ? 6 : 9;
+  static constexpr int R = W;              // ring slots per warp
+  static constexpr int D = W - 2;          // rows prefetched ahead of the one being consumed
   static constexpr int ROWB = 64 * 8 + 64 * 4;   // one row of a strip: 64 complex64 + 64 float32
   static constexpr int WARPS = 4;
   static constexpr int NT = 32 * WARPS;
   static constexpr size_t SMEM = (size_t)WARPS * R * ROWB;
-  static_assert(R >= D + 2 && (R & (R - 1)) == 0, "ring");
+  static_assert(W >= 4 * K + 1 && R >= D + 2, "window and ring");
 };
 
 // Per-warp constants of an item: broadcast pairs of the step coefficients (pre-multiplied by
@@ -74,6 +77,15 @@ __device__ __forceinline__ void cp_async_sz(uint32_t dst, const void* src, uint3
 template <int N>
 __device__ __forceinline__ void cp_async_wait_group() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// Predicated global stores of a node pair and of one node (no branch around them).
+__device__ __forceinline__ void st_pair_if(bool p, float2* dst, float a, float b, float c, float d) {
+  asm volatile("{ .reg .pred q; setp.ne.b32 q, %0, 0; @q st.global.v4.f32 [%1], {%2, %3, %4, %5}; }"
+               ::"r"((int)p), "l"(dst), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
+}
+__device__ __forceinline__ void st_node_if(bool p, float2* dst, float a, float b) {
+  asm volatile("{ .reg .pred q; setp.ne.b32 q, %0, 0; @q st.global.v2.f32 [%1], {%2, %3}; }"
+               ::"r"((int)p), "l"(dst), "f"(a), "f"(b) : "memory");
 }
 
 // Slope of one stage at the centre row of the window (slot C), pre-multiplied by dt/2:
@@ -105,7 +117,7 @@ __device__ __forceinline__ void stream_slope(const float2 (&inX)[W], const float
     mX = fma2(c.w2, s2X, mul2(c.w1, s1X));
     nmY = fma2(c.nw2, s2Y, mul2(c.nw1, s1Y));
   }
-  const float2 sq = f2(__fmaf_rn(X.x, X.x, Y.x * Y.x), __fmaf_rn(X.y, X.y, Y.y * Y.y));
+  const float2 sq = fma2(X, X, mul2(Y, Y));
   const float2 den = fma2(c.c14, sq, c.c13);
   const float2 r = mul2(pcv, f2(rcp_approx(den.x), rcp_approx(den.y)));
   const float2 a = fma2(c.c3, r, c.nc4);
@@ -139,11 +151,13 @@ __global__ void __launch_bounds__(StreamCfg<K>::NT, K == 1 ? NLSG_STREAM_MINB_K1
 rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ items, int n_items, int j_step,
               unsigned* __restrict__ counter) {
   typedef StreamCfg<K> G;
-  constexpr int W = G::W, D = G::D, R = G::R;
+  constexpr int W = G::W, D = G::D;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t ring = smem_u32(smem_raw + (size_t)warp * R * G::ROWB);
-  const unsigned char* ring_g = smem_raw + (size_t)warp * R * G::ROWB;
+  // this lane's bytes of ring slot 0 (state pair, pump pair); slot s is ROWB * s further
+  unsigned char* const ring_u = smem_raw + (size_t)warp * G::R * G::ROWB + lane * 16;
+  unsigned char* const ring_p = smem_raw + (size_t)warp * G::R * G::ROWB + 512 + lane * 8;
+  const uint32_t ring_u32 = smem_u32(ring_u), ring_p32 = smem_u32(ring_p);
 
   auto fetch = [&]() -> int {
     unsigned v = 0;
@@ -166,6 +180,9 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
     if (even != EVEN) continue;
     const int x = (int)it.x0 + 2 * lane;
     const bool in0 = x < n, in1 = x + 1 < n;
+    const bool out0 = in0 && x >= (int)it.ox0 && x < (int)it.ox1;
+    const bool out1 = in1 && x + 1 >= (int)it.ox0 && x + 1 < (int)it.ox1;
+    const int y0 = it.y0, y1 = it.y1;
     // per-lane column offsets clamped into the grid (a lane beyond it copies zero bytes from
     // column 0) and the byte counts of its copies
     const float2* __restrict__ src0 = src + (in0 ? x : 0);
@@ -174,9 +191,6 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
     const float* __restrict__ P1 = Pg + (in1 ? x + 1 : 0);
     const uint32_t szu0 = EVEN ? (in0 ? 16u : 0u) : (in0 ? 8u : 0u), szu1 = in1 ? 8u : 0u;
     const uint32_t szp0 = EVEN ? (in0 ? 8u : 0u) : (in0 ? 4u : 0u), szp1 = in1 ? 4u : 0u;
-    const bool out0 = in0 && x >= (int)it.ox0 && x < (int)it.ox1;
-    const bool out1 = in1 && x + 1 >= (int)it.ox0 && x + 1 < (int)it.ox1;
-    const int y0 = it.y0, y1 = it.y1;
 
     StreamConst c;
     {
@@ -209,21 +223,23 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
     // this segment needs, and whose prefetch row lies inside the grid and the segment: no checks
     const int clean_lo = y0 + 4 * K, clean_hi = (n < ie ? n : ie) - D;
 
-    // cp.async of row `row` into its ring slot; every lane copies its own node pair.  FULL: the
-    // row is known to lie inside the grid; otherwise rows beyond it arrive zero-filled.
-    auto issue_row = [&](int row, auto FULLc) {
+    // cp.async of one row into ring slot SLOT, the row at element offset roff (row * n) from the
+    // lane's columns; every lane copies its own node pair.  FULL: the row lies inside the grid;
+    // otherwise rows beyond it arrive zero-filled.
+    auto issue_row = [&](auto SLOTc, auto FULLc, int row, uint32_t roff) {
+      constexpr int SLOT = decltype(SLOTc)::value;
       constexpr bool FULL = decltype(FULLc)::value;
-      const uint32_t slot = ring + (uint32_t)((row & (R - 1)) * G::ROWB);
       const bool rin = FULL || row < n;
-      const size_t q = (size_t)(rin ? row : 0) * n;
+      const uint32_t o = rin ? roff : 0u;
+      const uint32_t du = ring_u32 + SLOT * G::ROWB, dp = ring_p32 + SLOT * G::ROWB;
       if (EVEN) {
-        cp_async_sz<16>(slot + lane * 16, src0 + q, rin ? szu0 : 0u);
-        cp_async_sz<8>(slot + 512 + lane * 8, P0 + q, rin ? szp0 : 0u);
+        cp_async_sz<16>(du, src0 + o, rin ? szu0 : 0u);
+        cp_async_sz<8>(dp, P0 + o, rin ? szp0 : 0u);
       } else {
-        cp_async_sz<8>(slot + lane * 16, src0 + q, rin ? szu0 : 0u);
-        cp_async_sz<8>(slot + lane * 16 + 8, src1 + q, rin ? szu1 : 0u);
-        cp_async_sz<4>(slot + 512 + lane * 8, P0 + q, rin ? szp0 : 0u);
-        cp_async_sz<4>(slot + 512 + lane * 8 + 4, P1 + q, rin ? szp1 : 0u);
+        cp_async_sz<8>(du, src0 + o, rin ? szu0 : 0u);
+        cp_async_sz<8>(du + 8, src1 + o, rin ? szu1 : 0u);
+        cp_async_sz<4>(dp, P0 + o, rin ? szp0 : 0u);
+        cp_async_sz<4>(dp + 4, P1 + o, rin ? szp1 : 0u);
       }
     };
 
@@ -234,31 +250,39 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
       w.t2X[s] = w.t2Y[s] = w.t3X[s] = w.t3Y[s] = w.t4X[s] = w.t4Y[s] = f2(0.f, 0.f);
     }
 
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      if (ib + d < ie) issue_row(ib + d, std::false_type{});
+    // element offsets (row * n) of the next row to prefetch (row ib first) and of the row stage 4
+    // writes (negative only in iterations that write nothing)
+    uint32_t roff = (uint32_t)ib * (uint32_t)n;
+    int soff = (ib - 4 * K) * n;
+    float2* const dst0 = dst + x;
+    StaticFor<0, D>::run([&](auto Dc) {
+      constexpr int d = decltype(Dc)::value;
+      if (ib + d < ie) issue_row(std::integral_constant<int, d>{}, std::false_type{}, ib + d, roff);
       async_commit();
-    }
+      roff += (uint32_t)n;
+    });
 
-    // One iteration of the wavefront at row i; P = (i - ib) mod W.  CHECK: decide per stage whether
-    // its row is needed by this segment (skip it otherwise) and zero stage values of rows beyond
-    // the grid (rows before the grid keep the zeros the windows start with).
+    // One iteration of the wavefront at row i, unroll phase P = (i - ib) mod W (also row i's ring
+    // slot).  CHECK: decide per stage whether its row is needed by this segment (skip it
+    // otherwise) and zero stage values of rows beyond the grid (rows before the grid keep the
+    // zeros the windows start with).
     auto iter = [&](int i, auto Pc, auto CHECKc) {
       constexpr int P = decltype(Pc)::value;
       constexpr bool CHECK = decltype(CHECKc)::value;
-      // row i: wait for its copy, move it into the window, prefetch row i + D
+      // row i: wait for its copy, move it into the window, prefetch row i + D into slot P + D
       cp_async_wait_group<D - 1>();
       {
-        const unsigned char* rs = ring_g + (i & (R - 1)) * G::ROWB;
-        const float4 v = *reinterpret_cast<const float4*>(rs + lane * 16);
-        const float2 p = *reinterpret_cast<const float2*>(rs + 512 + lane * 8);
+        const float4 v = *reinterpret_cast<const float4*>(ring_u + P * G::ROWB);
+        const float2 p = *reinterpret_cast<const float2*>(ring_p + P * G::ROWB);
         w.uX[P] = f2(v.x, v.z);
         w.uY[P] = f2(v.y, v.w);
         w.pc[P] = mul2(c.c12, p);
       }
-      if (!CHECK) issue_row(i + D, std::true_type{});
-      else if (i + D < ie) issue_row(i + D, std::false_type{});
+      constexpr int SN = (P + D) % W;
+      if (!CHECK) issue_row(std::integral_constant<int, SN>{}, std::true_type{}, i + D, roff);
+      else if (i + D < ie) issue_row(std::integral_constant<int, SN>{}, std::false_type{}, i + D, roff);
       async_commit();
+      roff += (uint32_t)n;
 
       // stage 1 at row i - K: input u, output t2 = u + q1, a = q1
       {
@@ -314,7 +338,8 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
           w.t4Y[C] = fma2(c.two, qY, w.uY[C]);
         }
       }
-      // stage 4 at row i - 4K: input t4; u' = u + (q1 + 2 q2 + 2 q3 + q4) / 3, stored
+      // stage 4 at row i - 4K: input t4; u' = u + (q1 + 2 q2 + 2 q3 + q4) / 3, stored at the row
+      // offset soff (row i - 4K)
       {
         constexpr int C = ((P - 4 * K) % W + W) % W;
         const int r = i - 4 * K;
@@ -325,15 +350,16 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
           stream_slope<K, W, C>(w.t4X, w.t4Y, w.pc[C], c, qX, qY);
           const float2 nX = fma2(c.third, add2(w.aX[C], qX), w.uX[C]);
           const float2 nY = fma2(c.third, add2(w.aY[C], qY), w.uY[C]);
-          const size_t q = (size_t)r * n + x;
+          float2* const gst = dst0 + soff;
           if (EVEN) {
-            if (out0) *reinterpret_cast<float4*>(dst + q) = make_float4(nX.x, nY.x, nX.y, nY.y);
+            st_pair_if(out0, gst, nX.x, nY.x, nX.y, nY.y);
           } else {
-            if (out0) dst[q] = f2(nX.x, nY.x);
-            if (out1) dst[q + 1] = f2(nX.y, nY.y);
+            st_node_if(out0, gst, nX.x, nY.x);
+            st_node_if(out1, gst + 1, nX.y, nY.y);
           }
         }
       }
+      soff += n;
     };
 
     for (int b = ib; b < ie; b += W) {
