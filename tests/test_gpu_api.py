@@ -222,3 +222,26 @@ def test_checks_fed_by_device_reductions_match_the_host_loop(gpu, dim):
     di = checks.damping_integral(sol)
     assert abs(di - sol.getDampingIntegral()) <= 1e-10 * max(1.0, abs(di))
     assert checks.check_integral(sol) == (abs(sol.getDampingIntegral()) <= checks.TOLERANCE)
+
+
+def test_job_intake_feeds_the_pool(gpu):
+    """schedulr-shaped jobs served by a complex128 pool equal Model.solve() of the same jobs
+    (the reference worker's path, schedulr/workr.py:45-75) to the drop-in tolerance."""
+    import json
+    from nls_gb300.intake import JobQueue, job_model, run_jobs
+    from nls_gb300.serve import Pool
+    q = JobQueue()
+    descs = [{"power": 2.0, "num_nodes": 48, "num_iters": 60},
+             {"power": 3.5, "num_nodes": 40, "num_iters": 45, "order": 3},
+             {"power": 1.5, "model": "1d", "num_nodes": 300, "num_iters": 80}]
+    ids = q.post_jobs([json.dumps(d) for d in descs])
+    pool = Pool(dtype=np.complex128, budget_bytes=1 << 28, chunk_steps=25)
+    sols = run_jobs(q, pool, dtype=np.complex128)
+    pool.close()
+    assert sorted(sols) == ids and q.pending() == 0
+    for jid, d in zip(ids, descs):
+        assert q.job(jid).state == "done"
+        want = job_model(json.dumps(d)).solve().getSolution()
+        got = sols[jid].getSolution()
+        assert got.shape == want.shape
+        assert rel(got, want) <= 1e-10, (jid, rel(got, want))

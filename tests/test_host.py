@@ -249,3 +249,39 @@ def test_native_alias_binds_the_gpu_module_object():
                 sys.modules.pop(k, None)
             else:
                 sys.modules[k] = v
+
+
+def test_job_intake_table_and_http_routes():
+    """schedulr's job contract in process and over HTTP on 127.0.0.1 (no GPU work)."""
+    import json
+    import urllib.request
+    from nls_gb300.intake import JobQueue, job_model, serve_http
+    q = JobQueue()
+    ids = q.post_jobs([json.dumps({"power": 2.5}), {"power": 3.0, "num_nodes": 32, "num_iters": 10}])
+    assert ids == [1, 2] and q.pending() == 2
+    m = job_model(q.job(2).description)
+    assert (m.num_nodes, m.num_iters, m.order, m.dx) == (32, 10, 5, 0.2)
+    assert np.asarray(m.getInitialSolution()).shape == (32, 32)
+    m1 = job_model(q.job(1).description)
+    assert (m1.num_nodes, m1.num_iters, m1.dt) == (200, 2000, 2e-3)
+    xm = 20.0 / 199                                    # nearest grid point to the pump centre
+    np.testing.assert_allclose(m1.getPumping().max(), 2.5 * np.exp(-2 * xm ** 2 / (2 * 25.0)), rtol=1e-12)
+    srv = serve_http(q, port=0)
+    port = srv.server_address[1]
+    try:
+        def call(method, path, body=None):
+            data = json.dumps(body).encode() if body is not None else None
+            req = urllib.request.Request(f"http://127.0.0.1:{port}{path}", data=data, method=method,
+                                         headers={"Content-Type": "application/json"})
+            with urllib.request.urlopen(req) as r:
+                raw = r.read()
+                return r.status, (json.loads(raw) if raw else None)
+        assert call("POST", "/api/jobs", {"jobs": [json.dumps({"power": 1.0})]})[0] == 201
+        st, job = call("GET", "/api/job", {"worker_id": 7})
+        assert st == 200 and job["job_id"] == 1
+        st, listing = call("GET", "/api/jobs")
+        assert st == 200 and [j["id"] for j in listing["jobs"]] == [1]
+        assert call("POST", "/api/job", {"worker_id": 7, "job_id": 1})[0] == 204
+        assert q.job(1).state == "done" and q.pending() == 2
+    finally:
+        srv.shutdown()
