@@ -54,13 +54,14 @@ SHAPE_KERNELS = {
     9: "rk4_2d_reg 64x96, 12 warps x 8 rows", 10: "rk4_2d_reg 64x96, 8 warps x 12 rows",
     11: "rk4_2d_reg 64x64, 16 warps x 4 rows", 12: "rk4_2d_reg 64x72, 8 warps x 9 rows",
     13: "rk4_2d_reg 64x72, 12 warps x 6 rows", 14: "rk4_2d_reg 64x80, 8 warps x 10 rows",
+    15: "rk4_2d_stream, 64-column strips walked as a four-stage wavefront (cp.async row ring)",
 }
-DEFAULT_SHAPE_C64 = 10
+DEFAULT_SHAPE_C64 = 15
 
 
 def _traffic_per_node():
     """DRAM bytes per node per fused-step launch from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "rk4_2d_reg_c64_batch_mix.md")
+    p = os.path.join(ROOT, "profiles", "rk4_2d_stream_c64_batch_mix.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -592,7 +593,7 @@ def run_ours(args):
                           "frac": achieved / peak, "traffic": (tpn * nodes_2d if tpn else None),
                           "kernel": "; ".join(sorted({SHAPE_KERNELS.get(v if v > 0 else DEFAULT_SHAPE_C64, str(v))
                                                       for v in (sp.variant for sp in specs2)}))
-                                    + " (TMA prefetch); one launch per RK4 step over all 2-D tiles",
+                                    + "; one launch per RK4 step over every 2-D instance",
                           "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": launch_s * 1e6,
                           "peak_source": peak_source}
     b2.close()

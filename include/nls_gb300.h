@@ -51,7 +51,8 @@ typedef struct nls_pool nls_pool;
  * 6 = 64 x (64 + 8K) with output tiles exactly 64 rows high (512), 7 = the same region with 768
  * (order 3) or 640 (order 5) threads; register-resident tiles (complex64 only), region 64 wide:
  * 8 = 64x80 (512), 9 = 64x96 (384), 10 = 64x96 (256), 11 = 64x64 (512), 12 = 64x72 (256),
- * 13 = 64x72 (384), 14 = 64x80 (256). */
+ * 13 = 64x72 (384), 14 = 64x80 (256); 15 = streaming wavefront over 64-column strips (complex64
+ * only; the complex64 default). */
 typedef struct nls_problem {
   int dim;
   int n;

@@ -16,7 +16,11 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
+#include <functional>
+#include <queue>
 #include <utility>
 #include <vector>
 
@@ -727,34 +731,86 @@ static void segments(int n, int ly, std::vector<std::pair<int, int>>& out) {
   }
 }
 
-// Estimated makespan (in strip-row iterations) of the items that segment height ly gives over
-// `slots` warps: the mean load per warp plus half the longest item (the expected tail).
-static double stream_cost(const std::vector<int>& ns, int K, int ly, int64_t slots) {
-  std::vector<StripGeom> st;
+int stream_choose_ly_search(const std::vector<int>& ns, int K, int64_t slots);
+
+// Makespan (in row iterations) of the items that segment height ly gives, taken longest first by
+// `slots` warps that each take the next item when done (the kernel's dynamic schedule).  An item
+// costs its rows, the 4K rows of drain past its end and, below the grid's first row, 4K rows of
+// warm-up, plus a start-up of kStartup row iterations (taking the item, reading the instance,
+// waiting for the first prefetched row).
+static double stream_makespan(const std::vector<int>& ns, const std::vector<int>& nstrips, int K, int ly,
+                              int64_t slots, double bound) {
+  constexpr double kStartup = 8.0;
   std::vector<std::pair<int, int>> sg;
+  std::vector<double> cost;
   double total = 0.0, longest = 0.0;
-  for (int n : ns) {
-    stream_strips(n, K, st);
-    segments(n, ly, sg);
+  for (size_t k = 0; k < ns.size(); ++k) {
+    segments(ns[k], ly, sg);
     for (auto& g : sg) {
-      // iterations of the wavefront (warm-up and drain rows inside the grid included)
-      const double it = (double)(g.second - g.first) + (g.first > 0 ? 4 * K : 0) + 4 * K;
-      total += it * (double)st.size();
+      const double it = (double)(g.second - g.first) + 4 * K + (g.first > 0 ? 4 * K : 0) + kStartup;
+      for (int q = 0; q < nstrips[k]; ++q) cost.push_back(it);
+      total += it * nstrips[k];
       longest = std::max(longest, it);
     }
   }
-  return total / (double)std::max<int64_t>(1, slots) + 0.5 * longest;
+  slots = std::max<int64_t>(1, slots);
+  if ((int64_t)cost.size() <= slots) return longest;
+  const double lower = std::max(longest, total / (double)slots);
+  if (lower >= bound) return lower;          // cannot beat the best so far
+  std::sort(cost.begin(), cost.end(), std::greater<double>());
+  std::priority_queue<double, std::vector<double>, std::greater<double>> warps;
+  for (int64_t w = 0; w < slots; ++w) warps.push(0.0);
+  for (double c : cost) {
+    const double t = warps.top();
+    warps.pop();
+    warps.push(t + c);
+  }
+  double end = 0.0;
+  while (!warps.empty()) {
+    end = std::max(end, warps.top());
+    warps.pop();
+  }
+  return end;
 }
 
 int stream_choose_ly(const std::vector<int>& ns, int K, int64_t slots) {
+  // a single grid's choice depends only on (n, K, slots): remember it
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int64_t>, int> single;
+  if (ns.size() == 1) {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = single.find(std::make_tuple(ns[0], K, slots));
+    if (it != single.end()) return it->second;
+  }
+  const int ly = stream_choose_ly_search(ns, K, slots);
+  if (ns.size() == 1) {
+    std::lock_guard<std::mutex> lk(mu);
+    single[std::make_tuple(ns[0], K, slots)] = ly;
+  }
+  return ly;
+}
+
+int stream_choose_ly_search(const std::vector<int>& ns, int K, int64_t slots) {
   int nmax = 1;
   for (int n : ns) nmax = std::max(nmax, n);
+  std::vector<int> nstrips(ns.size());
+  std::vector<StripGeom> st;
+  for (size_t k = 0; k < ns.size(); ++k) {
+    stream_strips(ns[k], K, st);
+    nstrips[k] = (int)st.size();
+  }
+  // candidate heights: the largest grid split into 1..64 segments, and a coarse ladder below
+  std::vector<int> cand;
+  for (int seg = 1; seg <= 64; ++seg) cand.push_back(std::max(16, (nmax + seg - 1) / seg));
+  for (int ly = 16; ly < nmax; ly += (ly < 128 ? 8 : (ly < 512 ? 32 : 128))) cand.push_back(ly);
+  std::sort(cand.begin(), cand.end());
+  cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
   int best = nmax;
-  double best_c = stream_cost(ns, K, nmax, slots);
-  for (int ly = 16; ly < nmax; ly += (ly < 128 ? 8 : (ly < 512 ? 32 : 128))) {
-    const double cst = stream_cost(ns, K, ly, slots);
-    if (cst < best_c * 0.999) {
-      best_c = cst;
+  double best_c = stream_makespan(ns, nstrips, K, nmax, slots, 1e300);
+  for (int ly : cand) {
+    const double c = stream_makespan(ns, nstrips, K, ly, slots, best_c);
+    if (c < best_c * 0.999) {
+      best_c = c;
       best = ly;
     }
   }
