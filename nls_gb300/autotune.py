@@ -49,17 +49,24 @@ def bucket(n: int) -> int:
     return b
 
 
-def candidates(dim: int, dtype, n: int):
+def feasible_1d(n: int, cl: int, order: int, dtype) -> bool:
+    """The resident 1-D kernels' size rule: a segment of ceil(n / cl) nodes fits the CTA's limit
+    (4096 nodes complex64, 2048 complex128), a cluster also holding 8K halo nodes, K = (order-1)/2."""
+    if cl == 0:
+        return True                      # unfused stage kernels: any size
+    K = (order - 1) // 2
+    lim = 4096 if np.dtype(dtype) == np.dtype(np.complex64) else 2048
+    seg = -(-n // cl)
+    if cl == 1:
+        return 2 * K <= seg <= lim
+    return 1 < cl <= 16 and seg >= 4 * K and seg + 8 * K <= lim
+
+
+def candidates(dim: int, dtype, n: int, order: int = 5):
     c64 = np.dtype(dtype) == np.dtype(np.complex64)
     if dim == 2:
         return [15, 10, 12, 13, 14, 9, 8, 11, 6, 1, 7, 2, 3, 4, 5, 0] if c64 else [0, 3]
-    out = []
-    lim = 4096 if c64 else 2048
-    for cl in (1, 2, 4, 8, 16):
-        seg = -(-n // cl)
-        if seg <= lim and seg >= 6:
-            out.append(cl)
-    return out + [0]
+    return [cl for cl in (1, 2, 4, 8, 16) if feasible_1d(n, cl, order, dtype)] + [0]
 
 
 def _time_variant(dim, n, order, dtype, variant, steps, device):
@@ -133,7 +140,7 @@ def tune(dim: int, n: int, order: int, dtype=np.complex64, steps: int = 128, dev
     times = {}
     nb = bucket(n)
     timer = _time_batch if mode == "batch" else _time_variant
-    for v in candidates(dim, dtype, nb):
+    for v in candidates(dim, dtype, nb, order):
         if mode == "batch" and v == 0:
             continue          # the unfused path is a single-solve fallback
         try:
@@ -227,7 +234,7 @@ def apply(specs, dtype=np.complex64, device: int = 0, mode: str = "batch"):
         best_t = _time_mix_assigned([copy.copy(s) for s in specs], dtype, 32, device)
         for order, b in keys:
             group = [s for s in specs if s.dim == 1 and s.order == order and bucket(s.n) == b]
-            for v in candidates(1, dtype, b):
+            for v in candidates(1, dtype, b, order):
                 if v == 0 or v == group[0].variant:
                     continue
                 trial = [copy.copy(s) for s in specs]
@@ -271,7 +278,9 @@ def _time_mix_assigned(specs, dtype, steps, device):
 def assign(specs, choices):
     """Apply the choices ``apply`` returned (for one population) to other specs of the same
     population, e.g. the requests of a served stream: per size bucket, or the shared 2-D shape of
-    a stencil order ("2d/o3/mix").  Specs with no matching choice keep their variant."""
+    a stencil order ("2d/o3/mix").  Specs with no matching choice keep their variant.
+    A 1-D cluster size chosen on one size of a bucket that does not fit another size of it
+    becomes the smallest larger cluster that fits (or the built-in choice)."""
     for s in specs:
         key = f"{s.dim}d/o{s.order}/n<={bucket(s.n)}"
         mix = f"{s.dim}d/o{s.order}/mix"
@@ -279,4 +288,7 @@ def assign(specs, choices):
             s.variant = int(choices[key])
         elif mix in choices:
             s.variant = int(choices[mix])
+        if s.dim == 1 and s.variant > 0 and not feasible_1d(s.n, s.variant, s.order, np.complex64):
+            fit = [cl for cl in (1, 2, 4, 8, 16) if cl > s.variant and feasible_1d(s.n, cl, s.order, np.complex64)]
+            s.variant = fit[0] if fit else -1
     return specs

@@ -285,3 +285,15 @@ def test_job_intake_table_and_http_routes():
         assert q.job(1).state == "done" and q.pending() == 2
     finally:
         srv.shutdown()
+
+
+def test_autotune_assign_respects_1d_size_limits():
+    """A cluster size tuned on one size of a bucket is not applied where it does not fit."""
+    from nls_gb300 import autotune
+    from nls_gb300.batch import Spec
+    specs = [Spec(1, n, 5, 1e-4, 0.04, np.zeros(23)) for n in (4500, 8192, 6000)]
+    autotune.assign(specs, {"1d/o5/n<=8192": 2})
+    assert [s.variant for s in specs] == [2, 4, 2]
+    for s in specs:
+        assert autotune.feasible_1d(s.n, s.variant, 5, np.complex64)
+    assert not autotune.feasible_1d(8192, 2, 5, np.complex64) and autotune.feasible_1d(4096, 1, 5, np.complex64)
