@@ -44,20 +44,43 @@ struct StaticFor<E, E> {
   __device__ __forceinline__ static void run(F&&) {}
 };
 
+// Unroll period (= window length = ring depth) at order 3, and warps per CTA (the warps of a CTA
+// share nothing, so this only sets the granularity of occupancy).
+#ifndef NLSG_STREAM_W_K1
+#define NLSG_STREAM_W_K1 5
+#endif
+#ifndef NLSG_STREAM_WARPS
+#define NLSG_STREAM_WARPS 1
+#endif
+
+// Ring depth in blocks of W rows per order (the prefetch distance grows with it; registers do
+// not).  Order 3: two blocks (8 rows ahead; one block, 3 rows ahead, left the warps waiting for
+// their rows: 2.04e11 against 2.17e11 node-steps/s on a 4096^2 grid); order 5: one block (16 rows
+// ahead with two blocks was 6 % slower).
+#ifndef NLSG_STREAM_RING_K1
+#define NLSG_STREAM_RING_K1 2
+#endif
+#ifndef NLSG_STREAM_RING_K2
+#define NLSG_STREAM_RING_K2 1
+#endif
+
 template <int K>
 struct StreamCfg {
   static constexpr int H = 4 * K;          // horizontal halo of a strip edge inside the grid
-  // The loop is unrolled by W iterations; W is also the number of rows each window holds (at
-  // least 4K + 1) and the depth of the shared-memory row ring, so the ring slot of row i is the
-  // unroll phase (i - first row) mod W, a compile-time constant, and so is every slot offset.
-  static constexpr int W = K == 1 ? 6 : 9;
-  static constexpr int R = W;              // ring slots per warp
-  static constexpr int D = W - 2;          // rows prefetched ahead of the one being consumed
+  // W is the number of rows each register window holds (at least 4K + 1) and the unroll period,
+  // so the window slot of row i is the unroll phase (i - first row) mod W, a compile-time
+  // constant.  The shared-memory row ring holds M blocks of W rows: row i sits in block
+  // ((i - first row) / W) mod M at the same phase, so a ring address is a block base (one
+  // register, advanced once per W rows) plus a compile-time offset.
+  static constexpr int W = K == 1 ? NLSG_STREAM_W_K1 : 9;
+  static constexpr int M = K == 1 ? NLSG_STREAM_RING_K1 : NLSG_STREAM_RING_K2;
+  static constexpr int R = W * M;          // ring slots per warp
+  static constexpr int D = R - 2;          // rows prefetched ahead of the one being consumed
   static constexpr int ROWB = 64 * 8 + 64 * 4;   // one row of a strip: 64 complex64 + 64 float32
-  static constexpr int WARPS = 4;
+  static constexpr int WARPS = NLSG_STREAM_WARPS;   // independent warps per CTA
   static constexpr int NT = 32 * WARPS;
   static constexpr size_t SMEM = (size_t)WARPS * R * ROWB;
-  static_assert(W >= 4 * K + 1 && R >= D + 2, "window and ring");
+  static_assert(W >= 4 * K + 1 && R % W == 0 && R >= D + 2, "window and ring");
 };
 
 // Per-warp constants of an item: broadcast pairs of the step coefficients (pre-multiplied by
@@ -156,16 +179,16 @@ struct StreamWin {
 // moves as one 16-byte copy (state) and one 8-byte copy (pump) and is stored as one 16-byte store;
 // otherwise every node moves on its own.  Items of the other kind are skipped (the runtime
 // launches both instantiations over the same item list when a group mixes them).
-// CTAs per SM the register budget is sized for (order 3: 3 x 4 warps; order 5: 2 x 4 warps).
-#ifndef NLSG_STREAM_MINB_K1
-#define NLSG_STREAM_MINB_K1 3
+// Register cap a thread.  Order 3: 152, so 13 one-warp CTAs fit an SM's 64K registers (the 5-row
+// window fits without spilling; a minimum-blocks bound of 13 would make the compiler aim for 128
+// and spill); order 5: 255 (8 one-warp CTAs per SM).
+#ifndef NLSG_STREAM_MAXNREG_K1
+#define NLSG_STREAM_MAXNREG_K1 152
 #endif
-#ifndef NLSG_STREAM_MINB_K2
-#define NLSG_STREAM_MINB_K2 2
-#endif
+#define NLSG_STREAM_BOUNDS(K) __maxnreg__(K == 1 ? NLSG_STREAM_MAXNREG_K1 : 255)
 
 template <int K, bool EVEN>
-__global__ void __launch_bounds__(StreamCfg<K>::NT, K == 1 ? NLSG_STREAM_MINB_K1 : NLSG_STREAM_MINB_K2)
+__global__ void NLSG_STREAM_BOUNDS(K)
 rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ items, int n_items, int j_step,
               unsigned* __restrict__ counter) {
   typedef StreamCfg<K> G;
@@ -241,15 +264,15 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
     // this segment needs, and whose prefetch row lies inside the grid and the segment: no checks
     const int clean_lo = y0 + 4 * K, clean_hi = (n < ie ? n : ie) - D;
 
-    // cp.async of one row into ring slot SLOT, the row at element offset roff (row * n) from the
-    // lane's columns; every lane copies its own node pair.  FULL: the row lies inside the grid;
-    // otherwise rows beyond it arrive zero-filled.
-    auto issue_row = [&](auto SLOTc, auto FULLc, int row, uint32_t roff) {
+    // cp.async of one row into the ring slot at byte offset base + SLOT * ROWB, the row at element
+    // offset roff (row * n) from the lane's columns; every lane copies its own node pair.  FULL:
+    // the row lies inside the grid; otherwise rows beyond it arrive zero-filled.
+    auto issue_row = [&](uint32_t base, auto SLOTc, auto FULLc, int row, uint32_t roff) {
       constexpr int SLOT = decltype(SLOTc)::value;
       constexpr bool FULL = decltype(FULLc)::value;
       const bool rin = FULL || row < n;
       const uint32_t o = rin ? roff : 0u;
-      const uint32_t du = ring_u32 + SLOT * G::ROWB, dp = ring_p32 + SLOT * G::ROWB;
+      const uint32_t du = ring_u32 + base + SLOT * G::ROWB, dp = ring_p32 + base + SLOT * G::ROWB;
       if (EVEN) {
         cp_async_sz<16>(du, src0 + o, rin ? szu0 : 0u);
         cp_async_sz<8>(dp, P0 + o, rin ? szp0 : 0u);
@@ -275,30 +298,35 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
     float2* const dst0 = dst + x;
     StaticFor<0, D>::run([&](auto Dc) {
       constexpr int d = decltype(Dc)::value;
-      if (ib + d < ie) issue_row(std::integral_constant<int, d>{}, std::false_type{}, ib + d, roff);
+      if (ib + d < ie) issue_row(0u, std::integral_constant<int, d>{}, std::false_type{}, ib + d, roff);
       async_commit();
       roff += (uint32_t)n;
     });
+    // byte offsets of the ring block holding the current W rows and of the block before it
+    constexpr uint32_t BLK = (uint32_t)(W * G::ROWB), RING = (uint32_t)(G::R * G::ROWB);
+    uint32_t rb = 0, rbp = RING - BLK;
 
-    // One iteration of the wavefront at row i, unroll phase P = (i - ib) mod W (also row i's ring
-    // slot).  CHECK: decide per stage whether its row is needed by this segment (skip it
-    // otherwise) and zero stage values of rows beyond the grid (rows before the grid keep the
-    // zeros the windows start with).
+    // One iteration of the wavefront at row i, unroll phase P = (i - ib) mod W (row i's window
+    // slot and its slot within the current ring block).  CHECK: decide per stage whether its row
+    // is needed by this segment (skip it otherwise) and zero stage values of rows beyond the grid
+    // (rows before the grid keep the zeros the windows start with).
     auto iter = [&](int i, auto Pc, auto CHECKc) {
       constexpr int P = decltype(Pc)::value;
       constexpr bool CHECK = decltype(CHECKc)::value;
-      // row i: wait for its copy, move it into the window, prefetch row i + D into slot P + D
+      // row i: wait for its copy, move it into the window, prefetch row i + D (= i - 2 modulo the
+      // ring: phase P - 2 of this block, or of the previous block for P < 2)
       cp_async_wait_group<D - 1>();
       {
-        const float4 v = *reinterpret_cast<const float4*>(ring_u + P * G::ROWB);
-        const float2 p = *reinterpret_cast<const float2*>(ring_p + P * G::ROWB);
+        const float4 v = *reinterpret_cast<const float4*>(ring_u + rb + P * G::ROWB);
+        const float2 p = *reinterpret_cast<const float2*>(ring_p + rb + P * G::ROWB);
         w.uX[P] = f2(v.x, v.z);
         w.uY[P] = f2(v.y, v.w);
         w.pc[P] = mul2(c.c12, p);
       }
-      constexpr int SN = (P + D) % W;
-      if (!CHECK) issue_row(std::integral_constant<int, SN>{}, std::true_type{}, i + D, roff);
-      else if (i + D < ie) issue_row(std::integral_constant<int, SN>{}, std::false_type{}, i + D, roff);
+      constexpr int SN = (P + W - 2) % W;
+      const uint32_t nb = P >= 2 ? rb : rbp;
+      if (!CHECK) issue_row(nb, std::integral_constant<int, SN>{}, std::true_type{}, i + D, roff);
+      else if (i + D < ie) issue_row(nb, std::integral_constant<int, SN>{}, std::false_type{}, i + D, roff);
       async_commit();
       roff += (uint32_t)n;
 
@@ -306,12 +334,13 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
       {
         constexpr int C = ((P - K) % W + W) % W;
         const int r = i - K;
-        bool run = true;
-        if (CHECK) {
-          if (r >= n) { w.t2X[C] = w.t2Y[C] = f2(0.f, 0.f); run = false; }
-          else run = r >= 0 && r >= y0 - 3 * K && r < y1 + 3 * K;
-        }
-        if (run) {
+        const bool run = !CHECK || (r < n && r >= 0 && r >= y0 - 3 * K && r < y1 + 3 * K);
+        if (!run) {
+          // a stage that is not run still writes its slots (zero: the value rows outside the
+          // grid must hold, and never read by the rows this segment needs), so every slot is
+          // written once per window cycle on every path and dead until then
+          w.t2X[C] = w.t2Y[C] = w.aX[C] = w.aY[C] = f2(0.f, 0.f);
+        } else {
           float2 qX, qY;
           stream_slope<K, W, C>(w.uX, w.uY, w.pc[C], c, qX, qY);
           w.aX[C] = qX;
@@ -324,12 +353,10 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
       {
         constexpr int C = ((P - 2 * K) % W + W) % W;
         const int r = i - 2 * K;
-        bool run = true;
-        if (CHECK) {
-          if (r >= n) { w.t3X[C] = w.t3Y[C] = f2(0.f, 0.f); run = false; }
-          else run = r >= 0 && r >= y0 - 2 * K && r < y1 + 2 * K;
-        }
-        if (run) {
+        const bool run = !CHECK || (r < n && r >= 0 && r >= y0 - 2 * K && r < y1 + 2 * K);
+        if (!run) {
+          w.t3X[C] = w.t3Y[C] = f2(0.f, 0.f);
+        } else {
           float2 qX, qY;
           stream_slope<K, W, C>(w.t2X, w.t2Y, w.pc[C], c, qX, qY);
           if (NLSG_STREAM_SCALAR_UPDATE) {
@@ -349,12 +376,10 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
       {
         constexpr int C = ((P - 3 * K) % W + W) % W;
         const int r = i - 3 * K;
-        bool run = true;
-        if (CHECK) {
-          if (r >= n) { w.t4X[C] = w.t4Y[C] = f2(0.f, 0.f); run = false; }
-          else run = r >= 0 && r >= y0 - K && r < y1 + K;
-        }
-        if (run) {
+        const bool run = !CHECK || (r < n && r >= 0 && r >= y0 - K && r < y1 + K);
+        if (!run) {
+          w.t4X[C] = w.t4Y[C] = f2(0.f, 0.f);
+        } else {
           float2 qX, qY;
           stream_slope<K, W, C>(w.t3X, w.t3Y, w.pc[C], c, qX, qY);
           if (NLSG_STREAM_SCALAR_UPDATE) {
@@ -402,6 +427,8 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
           if (b + decltype(Pc)::value < ie) iter(b + decltype(Pc)::value, Pc, std::true_type{});
         });
       }
+      rbp = rb;
+      rb = rb + BLK == RING ? 0u : rb + BLK;
     }
     cp_async_wait_group<0>();
   }
