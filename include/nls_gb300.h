@@ -243,6 +243,23 @@ int nls_solve_2d_noalloc(int dtype, const nls_problem* problem, int64_t iters,
  * context stays usable.  Not for production use. */
 int nls_test_set_tile_tx_extra(int device, unsigned extra_bytes);
 
+/* No counterpart in the reference.  Test control of the failure path of the bounded dependency
+ * waits of the streaming 2-D kernel (variant 15) when one launch runs several steps: with
+ * extra_steps > 0 every such wait on `device` asks for extra_steps more published steps than
+ * will ever exist, so the first waiting warp gives up after its bounded wait (about a second),
+ * sets the context's status word, the other warps stop waiting, and the synchronising call
+ * returns NLS_ERR_TIMEOUT; 0 restores normal operation.  No fault is raised and the context
+ * stays usable.  Not for production use. */
+int nls_test_set_stream_dep_extra(int device, unsigned extra_steps);
+
+/* No counterpart in the reference.  Test control of the streaming 2-D kernel's launch schedule
+ * for lists set up after the call (single solves, batches, pool chunks): 0 = automatic (several
+ * RK4 steps per launch for order-3 lists of at least 1.5 items per resident warp whose grids all
+ * take the paired form), 1 = several steps per launch whenever the grids all take the paired form,
+ * 2 = one step per launch.  Results are identical either way.  Process-wide; not for production
+ * use. */
+int nls_test_set_stream_steps_per_launch(int mode);
+
 #ifdef __cplusplus
 }
 #endif

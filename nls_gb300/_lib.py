@@ -100,6 +100,8 @@ SIGNATURES = {
     "nls_pool_destroy": (_i, [_p]),
     "nls_solve_2d_noalloc": (_i, [_i, _pp, _i64, _p, _p, _p]),
     "nls_test_set_tile_tx_extra": (_i, [_i, ctypes.c_uint]),
+    "nls_test_set_stream_dep_extra": (_i, [_i, ctypes.c_uint]),
+    "nls_test_set_stream_steps_per_launch": (_i, [_i]),
 }
 
 _lib = None

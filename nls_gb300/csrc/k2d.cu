@@ -686,21 +686,32 @@ int stream_kind(int n, const void* u0, const void* u1, const void* P) {
 }
 
 template <int K>
-static void launch_s(int kinds, const Inst2D* d_insts, const StripItem* d_items, int n_items, int j_step, int grid,
-                     unsigned* counter, cudaStream_t s) {
+static void launch_s(int kinds, const StreamLaunch& L, int j0, int nsteps, int grid, cudaStream_t s) {
   typedef StreamCfg<K> G;
-  if (kinds & STREAM_EVEN) rk4_2d_stream<K, true><<<grid, G::NT, G::SMEM, s>>>(d_insts, d_items, n_items, j_step, counter);
-  if (kinds & STREAM_ODD) rk4_2d_stream<K, false><<<grid, G::NT, G::SMEM, s>>>(d_insts, d_items, n_items, j_step, counter);
+  if (kinds & STREAM_EVEN)
+    rk4_2d_stream<K, true><<<grid, G::NT, G::SMEM, s>>>(L.insts, L.items, L.n_items, j0, nsteps, L.counter,
+                                                        L.dep_range, L.deps, L.flags, L.wait_flag);
+  if (kinds & STREAM_ODD)
+    rk4_2d_stream<K, false><<<grid, G::NT, G::SMEM, s>>>(L.insts, L.items, L.n_items, j0, nsteps, L.counter,
+                                                         L.dep_range, L.deps, L.flags, L.wait_flag);
 }
 
-cudaError_t launch_2d_stream(int K, int kinds, const Inst2D* d_insts, const StripItem* d_items, int n_items,
-                             int j_step, int grid, unsigned* counter, cudaStream_t s) {
-  if (n_items <= 0 || !(kinds & (STREAM_EVEN | STREAM_ODD))) return cudaSuccess;
-  if (!counter || grid <= 0) return cudaErrorInvalidValue;
-  if (K == 1) launch_s<1>(kinds, d_insts, d_items, n_items, j_step, grid, counter, s);
-  else if (K == 2) launch_s<2>(kinds, d_insts, d_items, n_items, j_step, grid, counter, s);
+cudaError_t launch_2d_stream(int K, int kinds, const StreamLaunch& L, int j0, int nsteps, int grid, cudaStream_t s) {
+  if (L.n_items <= 0 || nsteps <= 0 || !(kinds & (STREAM_EVEN | STREAM_ODD))) return cudaSuccess;
+  if (!L.counter || grid <= 0) return cudaErrorInvalidValue;
+  // several steps per launch: one kind only (the 16-byte paired copies bypass L1), a dependency
+  // list, flags, a status word, and a work index that fits an int
+  if (nsteps > 1 && (kinds != STREAM_EVEN || !L.dep_range || !L.deps || !L.flags || !L.wait_flag ||
+                     (int64_t)L.n_items * nsteps > INT32_MAX))
+    return cudaErrorInvalidValue;
+  if (K == 1) launch_s<1>(kinds, L, j0, nsteps, grid, s);
+  else if (K == 2) launch_s<2>(kinds, L, j0, nsteps, grid, s);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
+}
+
+cudaError_t stream_dep_extra_set(unsigned extra) {
+  return cudaMemcpyToSymbol(g_stream_dep_extra, &extra, sizeof(extra));
 }
 
 void stream_strips(int n, int K, std::vector<StripGeom>& out) {
@@ -826,6 +837,68 @@ void stream_items(int inst, int n, int K, int ly, std::vector<StripItem>& out) {
     for (auto& y : sg)
       out.push_back(StripItem{inst, (uint16_t)g.x0, (uint16_t)g.ox0, (uint16_t)g.ox1, (uint16_t)y.first,
                               (uint16_t)y.second, 0});
+}
+
+void stream_deps(const std::vector<StripItem>& items, const std::vector<int>& ns, int K, std::vector<int2>& range,
+                 std::vector<int>& deps) {
+  const int H = 4 * K;
+  range.assign(items.size(), int2{0, 0});
+  deps.clear();
+  // per instance: its strips (by x0) and segments (by y0), and the item at each (strip, segment)
+  std::map<int, std::vector<int>> by_inst;
+  for (size_t k = 0; k < items.size(); ++k) by_inst[items[k].inst].push_back((int)k);
+  std::vector<std::vector<int>> lists(items.size());
+  for (auto& kv : by_inst) {
+    const int n = ns[kv.first];
+    std::vector<int> xs, ys;
+    for (int k : kv.second) {
+      xs.push_back(items[k].x0);
+      ys.push_back(items[k].y0);
+    }
+    std::sort(xs.begin(), xs.end());
+    xs.erase(std::unique(xs.begin(), xs.end()), xs.end());
+    std::sort(ys.begin(), ys.end());
+    ys.erase(std::unique(ys.begin(), ys.end()), ys.end());
+    std::vector<int> at(xs.size() * ys.size(), -1);
+    auto sx = [&](int x0) { return (int)(std::lower_bound(xs.begin(), xs.end(), x0) - xs.begin()); };
+    auto sy = [&](int y0) { return (int)(std::lower_bound(ys.begin(), ys.end(), y0) - ys.begin()); };
+    for (int k : kv.second) at[(size_t)sx(items[k].x0) * ys.size() + sy(items[k].y0)] = k;
+    // read region: the strip's columns and the segment's rows widened by the 4K-row warm-up and
+    // drain; written region: the output columns and the segment's rows
+    auto rows_r = [&](const StripItem& a, int& r0, int& r1) {
+      r0 = std::max(0, (int)a.y0 - H);
+      r1 = std::min(n, (int)a.y1 + H);
+    };
+    auto meets = [](int a0, int a1, int b0, int b1) { return a0 < b1 && b0 < a1; };
+    for (int k : kv.second) {
+      const StripItem& a = items[k];
+      int ar0, ar1;
+      rows_r(a, ar0, ar1);
+      const int s = sx(a.x0);
+      // candidate segments: those starting before the widened rows end, from the first one that
+      // may reach them
+      for (int s2 = std::max(0, s - 2); s2 <= std::min((int)xs.size() - 1, s + 2); ++s2) {
+        int g0 = (int)(std::upper_bound(ys.begin(), ys.end(), std::max(0, ar0 - 1)) - ys.begin()) - 1;
+        g0 = std::max(0, g0);
+        for (int g = g0; g < (int)ys.size() && ys[g] < ar1 + 1; ++g) {
+          const int d = at[(size_t)s2 * ys.size() + g];
+          if (d < 0) continue;
+          const StripItem& b = items[d];
+          int br0, br1;
+          rows_r(b, br0, br1);
+          const int ac1 = std::min(n, (int)a.x0 + 64), bc1 = std::min(n, (int)b.x0 + 64);
+          const bool raw = meets(ar0, ar1, b.y0, std::min(n, (int)b.y1)) && meets(a.x0, ac1, b.ox0, b.ox1);
+          const bool war = meets(br0, br1, a.y0, std::min(n, (int)a.y1)) && meets(b.x0, bc1, a.ox0, a.ox1);
+          if (raw || war) lists[k].push_back(d);
+        }
+      }
+    }
+  }
+  for (size_t k = 0; k < items.size(); ++k) {
+    std::sort(lists[k].begin(), lists[k].end());
+    range[k] = int2{(int)deps.size(), (int)lists[k].size()};
+    deps.insert(deps.end(), lists[k].begin(), lists[k].end());
+  }
 }
 
 void stream_sort_items(std::vector<StripItem>& items) {

@@ -79,7 +79,8 @@ struct StreamCfg {
   static constexpr int ROWB = 64 * 8 + 64 * 4;   // one row of a strip: 64 complex64 + 64 float32
   static constexpr int WARPS = NLSG_STREAM_WARPS;   // independent warps per CTA
   static constexpr int NT = 32 * WARPS;
-  static constexpr size_t SMEM = (size_t)WARPS * R * ROWB;
+  // per warp: its row ring, then (after all rings) 16 bytes for the item being worked on
+  static constexpr size_t SMEM = (size_t)WARPS * R * ROWB + (size_t)WARPS * 16;
   static_assert(W >= 4 * K + 1 && R % W == 0 && R >= D + 2, "window and ring");
 };
 
@@ -100,6 +101,20 @@ __device__ __forceinline__ void cp_async_sz(uint32_t dst, const void* src, uint3
 template <int N>
 __device__ __forceinline__ void cp_async_wait_group() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// 16-byte copy that bypasses L1 (state rows written by other SMs earlier in the same launch must
+// not be served from a stale L1 line).
+__device__ __forceinline__ void cp_async_cg16(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst),
+               "l"(reinterpret_cast<uint64_t>(src)), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 // Predicated global stores of a node pair and of one node (no branch around them).
 __device__ __forceinline__ void st_pair_if(bool p, float2* dst, float a, float b, float c, float d) {
@@ -189,10 +204,30 @@ struct StreamWin {
 #endif
 #define NLSG_STREAM_BOUNDS(K) __maxnreg__(K == 1 ? NLSG_STREAM_MAXNREG_K1 : 255)
 
+// Bound of a dependency wait: polls with a back-off of up to 1 us, about one second in all.
+#ifndef NLSG_STREAM_WAIT_POLLS
+#define NLSG_STREAM_WAIT_POLLS (1u << 20)
+#endif
+
+// Added to every dependency a warp waits for (a test control: a large value makes every wait
+// expire, to exercise the timeout path).
+__device__ unsigned g_stream_dep_extra = 0;
+
+// One launch runs nsteps RK4 steps (j0 .. j0 + nsteps - 1) of every listed item.  Global work
+// index g = t * n_items + k is step t of item k; warps take g from counter[0] in order.  With
+// nsteps > 1, step t of item k first waits until every item in its dependency list (the items of
+// the same instance whose writes it reads, or whose reads it overwrites, in the ping-pong buffers)
+// has published step t - 1: flags[d] >= epoch + t, where epoch = counter[2] at launch (the number
+// of steps published before it; the last warp advances it by nsteps).  A warp only ever waits on
+// smaller indices, all taken by running warps, so the waits always end; each is also bounded
+// (about a second), after which the warp sets the context's status word and goes on (the state is
+// then wrong and the host reports the timeout), and warps that see the status word set stop
+// waiting.
 template <int K, bool EVEN>
 __global__ void NLSG_STREAM_BOUNDS(K)
-rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ items, int n_items, int j_step,
-              unsigned* __restrict__ counter) {
+rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ items, int n_items, int j0,
+              int nsteps, unsigned* __restrict__ counter, const int2* __restrict__ dep_range,
+              const int* __restrict__ deps, unsigned* __restrict__ flags, int* __restrict__ wait_flag) {
   typedef StreamCfg<K> G;
   constexpr int W = G::W, D = G::D;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -208,10 +243,46 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
     return (int)__shfl_sync(0xffffffffu, v, 0);
   };
 
-  for (int idx = fetch(); idx < n_items; idx = fetch()) {
+  const bool multi = nsteps > 1;
+  // the flag index and value this warp publishes when its item is done (kept in shared memory,
+  // out of the registers of the row loop)
+  volatile unsigned* const pub = reinterpret_cast<volatile unsigned*>(smem_raw + (size_t)G::WARPS * G::R * G::ROWB) +
+                                 4 * warp;
+  const int total = n_items * nsteps;
+  for (int g = fetch(); g < total; g = fetch()) {
+    const int t = multi ? g / n_items : 0;
+    const int idx = g - t * n_items;
+    const int j_step = j0 + t;
+    const unsigned epoch = multi ? *reinterpret_cast<volatile unsigned*>(&counter[2]) : 0u;
+    if (multi && lane == 0) {
+      pub[0] = (unsigned)idx;
+      pub[1] = epoch + (unsigned)t + 1u;
+    }
+    if (multi && t > 0) {
+      // wait for the dependencies' step t - 1 (32 flags per poll, one per lane)
+      const int2 dr = dep_range[idx];
+      const unsigned need = epoch + (unsigned)t + g_stream_dep_extra;
+      for (int base = 0; base < dr.y; base += 32) {
+        const int d = base + lane < dr.y ? deps[dr.x + base + lane] : -1;
+        unsigned ns = 32, polls = 0;
+        while (true) {
+          const bool ok = d < 0 || (int)(ld_acquire_gpu(&flags[d]) - need) >= 0;
+          if (__all_sync(0xffffffffu, ok)) break;
+          if (*reinterpret_cast<volatile int*>(wait_flag)) break;   // another warp timed out
+          if (++polls >= NLSG_STREAM_WAIT_POLLS) {
+            if (lane == 0) atomicExch(wait_flag, 1);
+            break;
+          }
+          __nanosleep(ns);
+          ns = ns < 1024 ? 2 * ns : 1024;
+        }
+      }
+      __syncwarp();
+    }
+    {
     const StripItem it = items[idx];
     const Inst2D& I = insts[it.inst];
-    if ((int64_t)j_step >= I.steps) continue;
+    if ((int64_t)j_step >= I.steps) goto published;
     const int n = I.n;
     const int par = (I.parity + j_step) & 1;
     const float2* __restrict__ src = reinterpret_cast<const float2*>(I.u[par]);
@@ -220,7 +291,7 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
     const bool even = !(n & 1) &&
                       ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst) |
                         reinterpret_cast<uintptr_t>(Pg)) & 15) == 0;
-    if (even != EVEN) continue;
+    if (even != EVEN) goto published;
     const int x = (int)it.x0 + 2 * lane;
     const bool in0 = x < n, in1 = x + 1 < n;
     const bool out0 = in0 && x >= (int)it.ox0 && x < (int)it.ox1;
@@ -276,7 +347,7 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
       const uint32_t o = rin ? roff : 0u;
       const uint32_t du = ring_u32 + base + SLOT * G::ROWB, dp = ring_p32 + base + SLOT * G::ROWB;
       if (EVEN) {
-        cp_async_sz<16>(du, src0 + o, rin ? szu0 : 0u);
+        cp_async_cg16(du, src0 + o, rin ? szu0 : 0u);
         cp_async_sz<8>(dp, P0 + o, rin ? szp0 : 0u);
       } else {
         cp_async_sz<8>(du, src0 + o, rin ? szu0 : 0u);
@@ -433,15 +504,25 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
       rb = rb + BLK == RING ? 0u : rb + BLK;
     }
     cp_async_wait_group<0>();
+    }
+  published:
+    if (multi) {
+      // this item's stores, then its flag (release: a warp that sees the flag sees the stores)
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) st_release_gpu(&flags[pub[0]], pub[1]);
+    }
   }
 
-  // every warp of the launch is done taking items: the last one resets the counter
+  // every warp of the launch is done taking items: the last one resets the counter (and advances
+  // the epoch past the steps this launch published)
   if (lane == 0) {
     __threadfence();
     const unsigned done = atomicAdd(&counter[1], 1u);
     if (done == gridDim.x * G::WARPS - 1) {
       counter[0] = 0u;
       counter[1] = 0u;
+      if (multi) counter[2] = counter[2] + (unsigned)nsteps;
       __threadfence();
     }
   }

@@ -83,8 +83,24 @@ enum { STREAM_EVEN = 1, STREAM_ODD = 2 };
 int stream_kind(int n, const void* u0, const void* u1, const void* P);
 int stream_2d_blocks_per_sm(int K);
 int stream_2d_warps_per_block();
-cudaError_t launch_2d_stream(int K, int kinds, const Inst2D* d_insts, const StripItem* d_items, int n_items,
-                             int j_step, int grid, unsigned* counter, cudaStream_t s);
+// Device data of one streaming work list: descriptors, items (longest first), the launch's counter
+// (3 words: next work index, warps done, epoch = steps published so far), and for launches of
+// several steps the dependency lists and one flag per item (zeroed with the counter when the list
+// is created) and the context's status word.
+struct StreamLaunch {
+  const Inst2D* insts;
+  const StripItem* items;
+  int n_items;
+  unsigned* counter;
+  const int2* dep_range;
+  const int* deps;
+  unsigned* flags;
+  int* wait_flag;
+};
+// RK4 steps j0 .. j0 + nsteps - 1 of every item in one launch (nsteps > 1 needs kinds ==
+// STREAM_EVEN and the dependency data).
+cudaError_t launch_2d_stream(int K, int kinds, const StreamLaunch& L, int j0, int nsteps, int grid, cudaStream_t s);
+cudaError_t stream_dep_extra_set(unsigned extra);
 // Strip geometry of an n-wide grid (first strip against the left edge, interior strips with a
 // 4K halo on both sides, last strip against the right edge), the segment height that minimises
 // the estimated makespan of a set of grids over `slots` warps, the items of one instance, and
@@ -96,6 +112,11 @@ void stream_strips(int n, int K, std::vector<StripGeom>& out);
 int stream_choose_ly(const std::vector<int>& ns, int K, int64_t slots);
 void stream_items(int inst, int n, int K, int ly, std::vector<StripItem>& out);
 void stream_sort_items(std::vector<StripItem>& items);
+// Dependency lists of a sorted item list (ns: grid side by instance): for item k every item of the
+// same instance whose written region meets k's read region, or whose read region meets k's written
+// region (k itself included); range[k] = {first, count} into deps.
+void stream_deps(const std::vector<StripItem>& items, const std::vector<int>& ns, int K, std::vector<int2>& range,
+                 std::vector<int>& deps);
 cudaError_t launch_2d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,
                             void* acc, void* dst, double dt, const PhysD& ph, const Stencil2D& op,
                             cudaStream_t st);

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <tuple>
@@ -261,6 +262,41 @@ static int64_t stream_slots(nls_ctx* ctx, int K) {
   return (int64_t)ctx->sm_count * std::max(1, stream_2d_blocks_per_sm(K)) * stream_2d_warps_per_block();
 }
 
+// Steps per launch of a streaming list that runs several steps per launch (bounded so that a
+// launch stays well under a second on the largest lists).
+static constexpr int kStreamStepsPerLaunch = 512;
+
+// Several steps per launch pay off where a warp finishing an item can take another whose
+// dependencies are met: lists of at least 1.5 items per resident warp (the batched mix: 1.9),
+// at order 3, whose grids all take the paired form.  Measured: the batched mix 2.04e11 ->
+// 2.23e11 node-steps/s; a single 4096^2 grid (one item per warp and step, so each step waits for
+// the previous one as at a launch boundary) 2.18e11 -> 1.84e11 at order 3, and at order 5, whose
+// nine-row loop body no longer fits the instruction cache once warps drift apart, 1.26e11 ->
+// 0.74e11.
+static std::atomic<int> g_stream_multi_mode{0};   // test control: 0 automatic, 1 always, 2 never
+static bool stream_multi_ok(nls_ctx* ctx, int K, int kinds, int n_items) {
+  if (kinds != STREAM_EVEN || n_items <= 0) return false;
+  const int mode = g_stream_multi_mode.load();
+  if (mode) return mode == 1;
+  return K == 1 && 2 * (int64_t)n_items >= 3 * stream_slots(ctx, K);
+}
+
+// Device layout of one streaming work list after its descriptors: items, counter (256 B),
+// dependency ranges, dependency indices, flags.
+struct StreamListLayout {
+  size_t items, counter, range, deps, flags, end;
+};
+static StreamListLayout stream_list_layout(size_t at, size_t n_items, size_t n_deps) {
+  StreamListLayout L;
+  L.items = at;
+  L.counter = L.items + align256(sizeof(StripItem) * std::max<size_t>(1, n_items));
+  L.range = L.counter + 256;
+  L.deps = L.range + align256(sizeof(int2) * std::max<size_t>(1, n_items));
+  L.flags = L.deps + align256(sizeof(int) * std::max<size_t>(1, n_deps));
+  L.end = L.flags + align256(sizeof(unsigned) * std::max<size_t>(1, n_items));
+  return L;
+}
+
 static int solve_2d_stream(nls_ctx* ctx, const nls_problem* pr, const Stencil2D& op, const PhysD& ph,
                            int64_t iters, const void* P, void* u) {
   const int n = pr->n;
@@ -275,31 +311,55 @@ static int solve_2d_stream(nls_ctx* ctx, const nls_problem* pr, const Stencil2D&
   std::vector<StripItem> items;
   stream_items(0, n, op.K, stream_choose_ly({n}, op.K, stream_slots(ctx, op.K)), items);
   stream_sort_items(items);
-  const int n_items = (int)items.size();
-  const size_t ib = align256(sizeof(Inst2D));
-  const size_t tb = align256(sizeof(StripItem) * n_items);
-  CK(ctx, ctx->desc.ensure(ib + tb + 256));
-  Inst2D* dI = (Inst2D*)ctx->desc.p;
-  StripItem* dT = (StripItem*)((char*)ctx->desc.p + ib);
-  unsigned* counter = (unsigned*)((char*)ctx->desc.p + ib + tb);
-  CK(ctx, cudaMemcpyAsync(dI, &I, sizeof(I), cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(dT, items.data(), sizeof(StripItem) * n_items, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned), ctx->stream));
-  const int grid = stream_grid(ctx, op.K, n_items);
   const int kinds = stream_kind(n, I.u[0], I.u[1], P);
-  const int S = 64;  // even: a replay returns the state to the caller's buffer
-  CK(ctx, replay(ctx, iters / S, [&]() -> cudaError_t {
-       for (int j = 0; j < S; ++j) {
-         cudaError_t e = launch_2d_stream(op.K, kinds, dI, dT, n_items, j, grid, counter, ctx->stream);
-         if (e) return e;
-       }
-       return cudaSuccess;
-     }));
-  const int64_t rem = iters % S;
-  for (int64_t j = 0; j < rem; ++j)
-    CK(ctx, launch_2d_stream(op.K, kinds, dI, dT, n_items, (int)j, grid, counter, ctx->stream));
-  if (rem & 1) CK(ctx, cudaMemcpyAsync(u, ctx->scratch.p, N * csize(NLS_C64), cudaMemcpyDeviceToDevice, ctx->stream));
-  ctx->launches += iters;
+  const int n_items = (int)items.size();
+  const bool multi = stream_multi_ok(ctx, op.K, kinds, n_items);
+  std::vector<int2> range;
+  std::vector<int> deps;
+  if (multi) stream_deps(items, {n}, op.K, range, deps);
+  const size_t ib = align256(sizeof(Inst2D));
+  const StreamListLayout Ly = stream_list_layout(ib, items.size(), deps.size());
+  CK(ctx, ctx->desc.ensure(Ly.end));
+  char* base = (char*)ctx->desc.p;
+  CK(ctx, cudaMemcpyAsync(base, &I, sizeof(I), cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(base + Ly.items, items.data(), sizeof(StripItem) * n_items, cudaMemcpyHostToDevice,
+                          ctx->stream));
+  CK(ctx, cudaMemsetAsync(base + Ly.counter, 0, 256, ctx->stream));
+  StreamLaunch L{(const Inst2D*)base, (const StripItem*)(base + Ly.items), n_items, (unsigned*)(base + Ly.counter),
+                 nullptr, nullptr, nullptr, ctx->wait_flag};
+  if (multi) {
+    CK(ctx, cudaMemcpyAsync(base + Ly.range, range.data(), sizeof(int2) * n_items, cudaMemcpyHostToDevice,
+                            ctx->stream));
+    CK(ctx, cudaMemcpyAsync(base + Ly.deps, deps.data(), sizeof(int) * deps.size(), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    CK(ctx, cudaMemsetAsync(base + Ly.flags, 0, sizeof(unsigned) * n_items, ctx->stream));
+    L.dep_range = (const int2*)(base + Ly.range);
+    L.deps = (const int*)(base + Ly.deps);
+    L.flags = (unsigned*)(base + Ly.flags);
+  }
+  const int grid = stream_grid(ctx, op.K, n_items);
+  if (multi) {
+    // whole chunks of steps per launch; the state alternates buffers each step
+    for (int64_t j = 0; j < iters;) {
+      const int s = (int)std::min<int64_t>(kStreamStepsPerLaunch, iters - j);
+      CK(ctx, launch_2d_stream(op.K, kinds, L, (int)(j & 1), s, grid, ctx->stream));
+      ctx->launches += 1;
+      j += s;
+    }
+  } else {
+    const int S = 64;  // even: a replay returns the state to the caller's buffer
+    CK(ctx, replay(ctx, iters / S, [&]() -> cudaError_t {
+         for (int j = 0; j < S; ++j) {
+           cudaError_t e = launch_2d_stream(op.K, kinds, L, j, 1, grid, ctx->stream);
+           if (e) return e;
+         }
+         return cudaSuccess;
+       }));
+    const int64_t rem = iters % S;
+    for (int64_t j = 0; j < rem; ++j) CK(ctx, launch_2d_stream(op.K, kinds, L, (int)j, 1, grid, ctx->stream));
+    ctx->launches += iters * ((kinds & STREAM_EVEN ? 1 : 0) + (kinds & STREAM_ODD ? 1 : 0));
+  }
+  if (iters & 1) CK(ctx, cudaMemcpyAsync(u, ctx->scratch.p, N * csize(NLS_C64), cudaMemcpyDeviceToDevice, ctx->stream));
   return NLS_OK;
 }
 
@@ -557,12 +617,14 @@ struct Group2D {
   int n_items = 0;
   bool tma = false;
   char* maps = nullptr;    // 3 tensor maps per member (TMA path)
-  // streaming step (TILE_STREAM): strip items of every member, longest first, and the
-  // launch-wide item counter
+  // streaming step (TILE_STREAM): strip items of every member, longest first, the launch-wide
+  // item counter, and the dependency lists and flags of launches of several steps
   std::vector<StripItem> sitems_h;
-  StripItem* sitems = nullptr;
-  unsigned* counter = nullptr;
+  std::vector<int2> range_h;
+  std::vector<int> deps_h;
+  StreamLaunch sl{};
   int kinds = 0;           // STREAM_EVEN / STREAM_ODD forms its members need
+  bool multi = false;      // several steps per launch
 };
 
 struct Member {
@@ -681,8 +743,9 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
       G.sitems_h.clear();
       for (size_t k = 0; k < G.idx.size(); ++k) stream_items((int)k, ns[k], G.K, ly, G.sitems_h);
       stream_sort_items(G.sitems_h);
+      stream_deps(G.sitems_h, ns, G.K, G.range_h, G.deps_h);
       items = (int)G.sitems_h.size();
-      item_bytes = align256(sizeof(StripItem) * std::max(1, items)) + 256;   // + the item counter
+      item_bytes = stream_list_layout(0, G.sitems_h.size(), G.deps_h.size()).end;
     } else {
       for (int i : G.idx) {
         const int tx = tile_out_x(G.shape, G.K), ty = tile_out_y(G.shape, G.K), n = b->m[i].pr.n;
@@ -710,11 +773,19 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
     Group2D& G = b->g2[g];
     G.d = (Inst2D*)(b->mem + g2off[g]);
     if (G.shape == TILE_STREAM) {
-      G.sitems = (StripItem*)(b->mem + g2items[g]);
-      G.counter = (unsigned*)(b->mem + g2items[g] + align256(sizeof(StripItem) * std::max(1, G.n_items)));
-      if (G.n_items)
-        CK(ctx, cudaMemcpyAsync(G.sitems, G.sitems_h.data(), sizeof(StripItem) * G.n_items, cudaMemcpyHostToDevice,
-                                ctx->stream));
+      // items, counter, dependency ranges and lists, flags (counter and flags zeroed with the block)
+      const StreamListLayout Ly = stream_list_layout(g2items[g], G.sitems_h.size(), G.deps_h.size());
+      G.sl = StreamLaunch{G.d, (const StripItem*)(b->mem + Ly.items), G.n_items, (unsigned*)(b->mem + Ly.counter),
+                          (const int2*)(b->mem + Ly.range), (const int*)(b->mem + Ly.deps),
+                          (unsigned*)(b->mem + Ly.flags), ctx->wait_flag};
+      if (G.n_items) {
+        CK(ctx, cudaMemcpyAsync(b->mem + Ly.items, G.sitems_h.data(), sizeof(StripItem) * G.n_items,
+                                cudaMemcpyHostToDevice, ctx->stream));
+        CK(ctx, cudaMemcpyAsync(b->mem + Ly.range, G.range_h.data(), sizeof(int2) * G.n_items,
+                                cudaMemcpyHostToDevice, ctx->stream));
+        CK(ctx, cudaMemcpyAsync(b->mem + Ly.deps, G.deps_h.data(), sizeof(int) * G.deps_h.size(),
+                                cudaMemcpyHostToDevice, ctx->stream));
+      }
       G.tma = false;
       G.grid = stream_grid(ctx, G.K, std::max(1, G.n_items));
       G.kinds = 0;
@@ -722,6 +793,7 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
         const Member& M = b->m[i];
         G.kinds |= stream_kind(M.pr.n, M.u[0], M.u[1], M.P);
       }
+      G.multi = stream_multi_ok(ctx, G.K, G.kinds, G.n_items);
       continue;
     }
     G.items = (TileItem*)(b->mem + g2items[g]);
@@ -796,6 +868,9 @@ static int batch_descriptors(nls_batch* b, int64_t steps) {
   return NLS_OK;
 }
 
+// A streaming group whose members all take the paired form runs many steps per launch.
+static bool stream_multi(const Group2D& G) { return G.shape == TILE_STREAM && G.multi; }
+
 static cudaError_t batch_sequence(nls_batch* b, int64_t steps) {
   nls_ctx* ctx = b->ctx;
   const int dtype = b->dtype;
@@ -813,10 +888,19 @@ static cudaError_t batch_sequence(nls_batch* b, int64_t steps) {
         return e;
     }
   }
+  // streaming groups whose members all take the paired form: many steps per launch
+  for (auto& G : b->g2)
+    if (stream_multi(G))
+      for (int64_t j = 0; j < steps;) {
+        const int s = (int)std::min<int64_t>(kStreamStepsPerLaunch, steps - j);
+        if ((e = launch_2d_stream(G.K, G.kinds, G.sl, (int)j, s, G.grid, ctx->stream))) return e;
+        j += s;
+      }
   for (int64_t j = 0; j < steps; ++j) {
     for (auto& G : b->g2)
-      if ((e = G.shape == TILE_STREAM
-                   ? launch_2d_stream(G.K, G.kinds, G.d, G.sitems, G.n_items, (int)j, G.grid, G.counter, ctx->stream)
+      if (!stream_multi(G) &&
+          (e = G.shape == TILE_STREAM
+                   ? launch_2d_stream(G.K, G.kinds, G.sl, (int)j, 1, G.grid, ctx->stream)
                : G.tma ? launch_2d_fused_tma(G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream,
                                              ctx->wait_flag)
                        : launch_2d_fused(dtype, G.K, G.shape, G.d, G.items, G.n_items, (int)j, G.grid, ctx->stream)))
@@ -856,7 +940,10 @@ static cudaError_t batch_sequence(nls_batch* b, int64_t steps) {
 }
 
 static int64_t batch_launches(const nls_batch* b, int64_t steps) {
-  int64_t l = (int64_t)b->g1.size() + steps * (int64_t)b->g2.size();
+  int64_t l = (int64_t)b->g1.size();
+  for (auto& G : b->g2)
+    l += stream_multi(G) ? (steps + kStreamStepsPerLaunch - 1) / kStreamStepsPerLaunch
+                         : steps * (G.shape == TILE_STREAM && G.kinds == (STREAM_EVEN | STREAM_ODD) ? 2 : 1);
   for (auto& M : b->m) if (M.kind == 3 || M.kind == 4) l += 4 * steps;
   return l;
 }
@@ -1156,6 +1243,17 @@ NLS_API int nls_batch_create(nls_ctx* ctx, int dtype, int count, const nls_probl
 NLS_API int nls_test_set_tile_tx_extra(int device, unsigned extra_bytes) {
   if (cudaSetDevice(device) != cudaSuccess) return NLS_ERR_CUDA;
   return tile_tx_extra_set(extra_bytes) == cudaSuccess ? NLS_OK : NLS_ERR_CUDA;
+}
+
+NLS_API int nls_test_set_stream_steps_per_launch(int mode) {
+  if (mode < 0 || mode > 2) return NLS_ERR_INVALID;
+  g_stream_multi_mode.store(mode);
+  return NLS_OK;
+}
+
+NLS_API int nls_test_set_stream_dep_extra(int device, unsigned extra_steps) {
+  if (cudaSetDevice(device) != cudaSuccess) return NLS_ERR_CUDA;
+  return stream_dep_extra_set(extra_steps) == cudaSuccess ? NLS_OK : NLS_ERR_CUDA;
 }
 
 NLS_API int nls_batch_set(nls_batch* b, int index, const void* pumping, const void* u0) {
@@ -1500,6 +1598,8 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
   const int buf = (int)(p->next_chunk & 1);
   // work items of each 2-D group: tiles, or strip items over the group's current mix
   std::vector<std::vector<StripItem>> sitems(g2.size());
+  std::vector<std::vector<int2>> sranges(g2.size());
+  std::vector<std::vector<int>> sdeps(g2.size());
   {
     size_t gi = 0;
     for (auto& kv : g2) {
@@ -1510,12 +1610,13 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
         const int ly = stream_choose_ly(ns, K, stream_slots(ctx, K));
         for (size_t k = 0; k < ns.size(); ++k) stream_items((int)k, ns[k], K, ly, sitems[gi]);
         stream_sort_items(sitems[gi]);
+        stream_deps(sitems[gi], ns, K, sranges[gi], sdeps[gi]);
       }
       ++gi;
     }
   }
-  // descriptor image: all groups back to back (a streaming group's item counter is part of the
-  // image and uploads as zero)
+  // descriptor image: all groups back to back (a streaming group's item counter and flags are
+  // part of the image and upload as zero)
   size_t bytes = 0;
   for (auto& kv : g1) bytes += align256(sizeof(Inst1D) * kv.second.size());
   {
@@ -1523,7 +1624,7 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
     for (auto& kv : g2) {
       if (std::get<1>(kv.first) == TILE_STREAM) {
         bytes += align256(sizeof(Inst2D) * kv.second.size()) +
-                 align256(sizeof(StripItem) * std::max<size_t>(1, sitems[gi].size())) + 256;
+                 stream_list_layout(0, sitems[gi].size(), sdeps[gi].size()).end;
       } else {
         int items = 0;
         for (int i : kv.second) items += p->slots[i].ntiles;
@@ -1537,7 +1638,7 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
   CK(ctx, p->d_desc[buf].ensure(bytes));
   char* d = (char*)p->d_desc[buf].p;
   struct L1 { int K, cl, seg, count; size_t off; };
-  struct L2 { int K, shape, n_items, grid; size_t off, off_items, off_counter; bool tma; int kinds; };
+  struct L2 { int K, shape, n_items, grid; size_t off, off_items; StreamListLayout ly; bool tma; int kinds; };
   std::vector<L1> l1;
   std::vector<L2> l2;
   size_t off = 0;
@@ -1566,10 +1667,14 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
     int items = 0;
     if (stream) items = (int)sitems[gi].size();
     else for (int i : kv.second) items += p->slots[i].ntiles;
-    const size_t moff = ioff + (stream ? align256(sizeof(StripItem) * std::max(1, items))
-                                       : align256(sizeof(TileItem) * items));
+    const StreamListLayout ly = stream_list_layout(ioff, stream ? sitems[gi].size() : 0, stream ? sdeps[gi].size() : 0);
+    const size_t moff = stream ? ly.end : ioff + align256(sizeof(TileItem) * items);
     TileItem* it = (TileItem*)(p->h_desc.data() + ioff);
-    if (stream && items) std::memcpy(p->h_desc.data() + ioff, sitems[gi].data(), sizeof(StripItem) * items);
+    if (stream && items) {
+      std::memcpy(p->h_desc.data() + ly.items, sitems[gi].data(), sizeof(StripItem) * items);
+      std::memcpy(p->h_desc.data() + ly.range, sranges[gi].data(), sizeof(int2) * items);
+      std::memcpy(p->h_desc.data() + ly.deps, sdeps[gi].data(), sizeof(int) * sdeps[gi].size());
+    }
     int q_items = 0, kinds = 0;
     for (size_t k = 0; k < kv.second.size(); ++k) {
       const Slot& S = p->slots[kv.second[k]];
@@ -1593,8 +1698,8 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
       const int occ = tma ? fused_2d_tma_blocks_per_sm(K, shape) : fused_2d_blocks_per_sm(dtype, K, shape);
       grid = std::max(1, std::min(items, ctx->sm_count * std::max(1, occ)));
     }
-    l2.push_back(L2{K, shape, items, grid, off, ioff, moff, tma, kinds});
-    off = moff + (stream ? 256 : align256(tma_map_bytes() * kv.second.size()));
+    l2.push_back(L2{K, shape, items, grid, off, ioff, ly, tma, kinds});
+    off = moff + (stream ? 0 : align256(tma_map_bytes() * kv.second.size()));
     ++gi;
   }
   // The previous user of this descriptor buffer is the chunk before the one in flight, already
@@ -1613,12 +1718,27 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
       ctx->launches += 1;
     }
   }
+  auto stream_of = [&](const L2& L) {
+    return StreamLaunch{(const Inst2D*)(d + L.off), (const StripItem*)(d + L.ly.items), L.n_items,
+                        (unsigned*)(d + L.ly.counter), (const int2*)(d + L.ly.range), (const int*)(d + L.ly.deps),
+                        (unsigned*)(d + L.ly.flags), ctx->wait_flag};
+  };
+  auto multi = [&](const L2& L) { return L.shape == TILE_STREAM && stream_multi_ok(ctx, L.K, L.kinds, L.n_items); };
+  // streaming groups whose members all take the paired form: the whole chunk in one launch
+  for (auto& L : l2)
+    if (multi(L))
+      for (int64_t j = 0; j < max_steps;) {
+        const int s = (int)std::min<int64_t>(kStreamStepsPerLaunch, max_steps - j);
+        CK(ctx, launch_2d_stream(L.K, L.kinds, stream_of(L), (int)j, s, L.grid, ctx->stream));
+        ctx->launches += 1;
+        j += s;
+      }
   for (int64_t j = 0; j < max_steps; ++j)
     for (auto& L : l2) {
+      if (multi(L)) continue;
       const Inst2D* dI = (const Inst2D*)(d + L.off);
       if (L.shape == TILE_STREAM) {
-        CK(ctx, launch_2d_stream(L.K, L.kinds, dI, (const StripItem*)(d + L.off_items), L.n_items, (int)j, L.grid,
-                                 (unsigned*)(d + L.off_counter), ctx->stream));
+        CK(ctx, launch_2d_stream(L.K, L.kinds, stream_of(L), (int)j, 1, L.grid, ctx->stream));
       } else {
         const TileItem* dT = (const TileItem*)(d + L.off_items);
         CK(ctx, L.tma ? launch_2d_fused_tma(L.K, L.shape, dI, dT, L.n_items, (int)j, L.grid, ctx->stream,

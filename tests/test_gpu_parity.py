@@ -465,6 +465,104 @@ def test_tile_wait_timeout_is_reported_and_the_context_recovers(gpu, oracle_lib)
     assert rel(got, want) <= 3e-5
 
 
+@pytest.fixture
+def stream_mode():
+    """Sets the streaming kernel's launch schedule (test control) for lists set up afterwards:
+    1 = several RK4 steps per launch wherever the grids take the paired form, 2 = one step per
+    launch; restores the automatic choice afterwards."""
+    from nls_gb300 import _lib
+
+    def set_mode(m):
+        assert _lib.lib().nls_test_set_stream_steps_per_launch(m) == _lib.NLS_OK
+    yield set_mode
+    set_mode(0)
+
+
+@pytest.mark.parametrize("order,n", [(3, 1000), (5, 516), (3, 130), (3, 64)])
+def test_2d_c64_stream_several_steps_per_launch_equal_single_steps(gpu, stream_mode, order, n):
+    """The streaming step with many RK4 steps per launch (an item of step t + 1 starts once the
+    items of step t it reads from or overwrites have published) equals one launch per step bit for
+    bit, at both orders (grids of even side: the paired form)."""
+    from nls_gb300 import device
+    s = _spec_2d(n, order)
+    iters = 37                                   # odd: the state ends in the scratch buffer
+    u0 = gpu.tensor(np.ascontiguousarray(np.asarray(s.u0).T), dtype=gpu.complex64, device="cuda")
+    P = gpu.tensor(np.ascontiguousarray(np.asarray(s.pumping).T), dtype=gpu.float32, device="cuda")
+    kw = dict(order=order, dt=s.dt, dx=s.dx, coeffs=s.coeffs, variant=15)
+    stream_mode(1)
+    a = u0.clone()
+    device.solve_(a, P, iters=iters, **kw)
+    stream_mode(2)
+    b = u0.clone()
+    device.solve_(b, P, iters=iters, **kw)
+    gpu.cuda.synchronize()
+    assert gpu.equal(a, b)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batch_stream_schedules_match_single_solves(gpu, stream_mode, mode):
+    """A batch whose square grids share the streaming kernel, run with several steps per launch (1)
+    and one step per launch (2), equals single solves bit for bit."""
+    from nls_gb300.batch import BatchSolver
+    specs = _mixed_specs(np.complex64)
+    for s in specs[:-1]:
+        if s.dim == 2:
+            s.variant = 15
+    stream_mode(mode)
+    b = BatchSolver(specs, dtype=np.complex64)
+    b.run(57)
+    b.run(20)
+    stream_mode(2)
+    for i, s in enumerate(specs):
+        want = _device_solve(gpu, s, 77, np.complex64, s.variant)
+        assert np.array_equal(b.get(i), want), i
+
+
+def test_pool_stream_several_steps_per_launch_match_single_solves(gpu, stream_mode):
+    """Pool chunks of the streaming kernel with several steps per launch, requests of different
+    step counts (a request stops at its own count inside a launch), equal single solves."""
+    from nls_gb300 import workloads as w
+    from nls_gb300.serve import Pool
+    stream_mode(1)
+    reqs = [(w.mix_instance(30 + i, 2, variant=15), 35 + 11 * i) for i in range(5)]
+    pool = Pool(budget_bytes=1 << 30, chunk_steps=40)
+    for tag, (spec, steps) in enumerate(reqs):
+        pool.admit(spec, steps, tag)
+    got = {}
+    while True:
+        r = pool.take_with_state()
+        if r is not None:
+            got[r[0]] = r[1]
+            continue
+        if pool.status()[0] == 0:
+            break
+        pool.step()
+    stream_mode(2)
+    for tag, (spec, steps) in enumerate(reqs):
+        want = _device_solve(gpu, spec, steps, np.complex64, 15)
+        assert np.array_equal(got[tag], want), tag
+
+
+def test_stream_dependency_wait_timeout_is_reported_and_the_context_recovers(gpu, oracle_lib, stream_mode):
+    """A launch of several streaming steps whose dependency waits can never be met (test control):
+    the first bounded wait gives up (about a second), the others stop waiting, the context's
+    synchronize reports NLS_ERR_TIMEOUT, and the next solve is correct."""
+    from nls_gb300 import _lib, device
+    s = _spec_2d(256, 3)
+    stream_mode(1)
+    assert _lib.lib().nls_test_set_stream_dep_extra(0, 1 << 30) == _lib.NLS_OK
+    try:
+        _device_solve(gpu, s, 3, np.complex64, 15)
+        with pytest.raises(_lib.NativeError) as err:
+            device.context(0).synchronize()
+        assert err.value.status == _lib.NLS_ERR_TIMEOUT
+    finally:
+        assert _lib.lib().nls_test_set_stream_dep_extra(0, 0) == _lib.NLS_OK
+    got = _device_solve(gpu, s, 40, np.complex64, 15)
+    want = oracle_lib.solve(s.dt, s.dx, 3, 40, s.pumping, s.coeffs, s.u0, dtype=np.float32)
+    assert rel(got, want) <= 3e-5
+
+
 @pytest.mark.parametrize("order,n", [(3, 1000), (5, 1000), (3, 1030), (5, 515)])
 def test_2d_c64_stream_large_grids(gpu, oracle_lib, order, n):
     """The streaming step on grids of many strips and row segments (segment warm-up and drain,
