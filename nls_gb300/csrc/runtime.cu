@@ -274,6 +274,14 @@ static constexpr int kStreamStepsPerLaunch = 512;
 // nine-row loop body no longer fits the instruction cache once warps drift apart, 1.26e11 ->
 // 0.74e11.
 static std::atomic<int> g_stream_multi_mode{0};   // test control: 0 automatic, 1 always, 2 never
+
+// Segment height of a streaming list over grids ns: the one-step-per-launch schedule simulation's
+// choice.  (Choosing instead the tallest height that gives 1.5 items per warp, so that single
+// large grids also run several steps per launch, measured: 4096^2 2.15e11 -> 2.18e11, 8192^2
+// 2.37e11 -> 2.13e11, the batched mix 2.23e11 -> 2.08e11 node-steps/s.)
+static int stream_plan_ly(nls_ctx* ctx, const std::vector<int>& ns, int K) {
+  return stream_choose_ly(ns, K, stream_slots(ctx, K));
+}
 static bool stream_multi_ok(nls_ctx* ctx, int K, int kinds, int n_items) {
   if (kinds != STREAM_EVEN || n_items <= 0) return false;
   const int mode = g_stream_multi_mode.load();
@@ -309,7 +317,7 @@ static int solve_2d_stream(nls_ctx* ctx, const nls_problem* pr, const Stencil2D&
   I.steps = INT64_MAX; I.dt = pr->dt; I.ph = ph; I.op = op;
   set_params(I);
   std::vector<StripItem> items;
-  stream_items(0, n, op.K, stream_choose_ly({n}, op.K, stream_slots(ctx, op.K)), items);
+  stream_items(0, n, op.K, stream_plan_ly(ctx, {n}, op.K), items);
   stream_sort_items(items);
   const int kinds = stream_kind(n, I.u[0], I.u[1], P);
   const int n_items = (int)items.size();
@@ -739,7 +747,7 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
     if (G.shape == TILE_STREAM) {
       std::vector<int> ns;
       for (int i : G.idx) ns.push_back(b->m[i].pr.n);
-      const int ly = stream_choose_ly(ns, G.K, stream_slots(ctx, G.K));
+      const int ly = stream_plan_ly(ctx, ns, G.K);
       G.sitems_h.clear();
       for (size_t k = 0; k < G.idx.size(); ++k) stream_items((int)k, ns[k], G.K, ly, G.sitems_h);
       stream_sort_items(G.sitems_h);
@@ -1607,7 +1615,7 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
       if (shape == TILE_STREAM) {
         std::vector<int> ns;
         for (int i : kv.second) ns.push_back(p->slots[i].pr.n);
-        const int ly = stream_choose_ly(ns, K, stream_slots(ctx, K));
+        const int ly = stream_plan_ly(ctx, ns, K);
         for (size_t k = 0; k < ns.size(); ++k) stream_items((int)k, ns[k], K, ly, sitems[gi]);
         stream_sort_items(sitems[gi]);
         stream_deps(sitems[gi], ns, K, sranges[gi], sdeps[gi]);
