@@ -232,6 +232,8 @@ rk4_2d_fused(const Inst2D* __restrict__ insts, const TileItem* __restrict__ item
     buf1[RY * RX + i] = mk<T>(0, 0);
   }
   const bool x_interior = x >= H && x < RX - H;
+  pdl_wait();      // the previous launch's states (programmatic launch)
+  pdl_trigger();
 
   auto active = [&](int idx) -> bool {
     return idx < n_items && (int64_t)j_step < insts[items[idx].inst].steps;
@@ -351,6 +353,8 @@ __global__ void __launch_bounds__(256) rk4_2d_stage(int n, int s, const void* __
                                                     void* __restrict__ acc_, void* __restrict__ dst_,
                                                     Params<T> prm) {
   typedef typename C2<T>::type C;
+  pdl_wait();
+  pdl_trigger();
   const int x = blockIdx.x * 32 + (threadIdx.x & 31);
   const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
   if (x >= n || y >= n) return;
@@ -477,9 +481,8 @@ template <typename T, int K, int RX, int RY, int NS, bool TMA = false>
 static cudaError_t launch_f(const Inst2D* d_insts, const TileItem* d_items, int n_items, int j_step,
                             int grid, cudaStream_t s, int* wait_flag = nullptr) {
   typedef TileCfg<T, K, RX, RY, NS> G;
-  auto kern = rk4_2d_fused<T, K, RX, RY, NS, TMA>;
-  kern<<<grid, G::NT, smem_f<T, K, RX, RY, NS, TMA>(), s>>>(d_insts, d_items, n_items, j_step, wait_flag);
-  return cudaGetLastError();
+  return launch_pdl(rk4_2d_fused<T, K, RX, RY, NS, TMA>, dim3(grid), dim3(G::NT), smem_f<T, K, RX, RY, NS, TMA>(), s,
+                    d_insts, d_items, n_items, j_step, wait_flag);
 }
 
 // Sets the shared-memory attribute (outside any capture) and returns CTAs per SM.
@@ -509,8 +512,8 @@ template <int K, int NW, int NJ, bool TMA>
 static cudaError_t launch_r(const Inst2D* d_insts, const TileItem* d_items, int n_items, int j_step,
                             int grid, cudaStream_t s, int* wait_flag = nullptr) {
   typedef RegCfg<K, NW, NJ> G;
-  rk4_2d_reg<K, NW, NJ, TMA><<<grid, G::NT, G::SMEM, s>>>(d_insts, d_items, n_items, j_step, wait_flag);
-  return cudaGetLastError();
+  return launch_pdl(rk4_2d_reg<K, NW, NJ, TMA>, dim3(grid), dim3(G::NT), G::SMEM, s, d_insts, d_items, n_items, j_step,
+                    wait_flag);
 }
 // Sets the shared-memory attribute (outside any capture) and returns CTAs per SM.
 template <int K, int NW, int NJ, bool TMA>
@@ -686,14 +689,25 @@ int stream_kind(int n, const void* u0, const void* u1, const void* P) {
 }
 
 template <int K>
-static void launch_s(int kinds, const StreamLaunch& L, int j0, int nsteps, int grid, cudaStream_t s) {
+static cudaError_t launch_s(int kinds, const StreamLaunch& L, int j0, int nsteps, int grid, cudaStream_t s) {
   typedef StreamCfg<K> G;
+  if (K != 1) {
+    if (kinds & STREAM_EVEN)
+      rk4_2d_stream<K, true><<<grid, G::NT, G::SMEM, s>>>(L.insts, L.items, L.n_items, j0, nsteps, L.counter,
+                                                          L.dep_range, L.deps, L.flags, L.wait_flag);
+    if (kinds & STREAM_ODD)
+      rk4_2d_stream<K, false><<<grid, G::NT, G::SMEM, s>>>(L.insts, L.items, L.n_items, j0, nsteps, L.counter,
+                                                           L.dep_range, L.deps, L.flags, L.wait_flag);
+    return cudaGetLastError();
+  }
+  cudaError_t e = cudaSuccess;
   if (kinds & STREAM_EVEN)
-    rk4_2d_stream<K, true><<<grid, G::NT, G::SMEM, s>>>(L.insts, L.items, L.n_items, j0, nsteps, L.counter,
-                                                        L.dep_range, L.deps, L.flags, L.wait_flag);
-  if (kinds & STREAM_ODD)
-    rk4_2d_stream<K, false><<<grid, G::NT, G::SMEM, s>>>(L.insts, L.items, L.n_items, j0, nsteps, L.counter,
-                                                         L.dep_range, L.deps, L.flags, L.wait_flag);
+    e = launch_pdl(rk4_2d_stream<K, true>, dim3(grid), dim3(G::NT), G::SMEM, s, L.insts, L.items, L.n_items, j0,
+                   nsteps, L.counter, L.dep_range, L.deps, L.flags, L.wait_flag);
+  if (!e && (kinds & STREAM_ODD))
+    e = launch_pdl(rk4_2d_stream<K, false>, dim3(grid), dim3(G::NT), G::SMEM, s, L.insts, L.items, L.n_items, j0,
+                   nsteps, L.counter, L.dep_range, L.deps, L.flags, L.wait_flag);
+  return e;
 }
 
 cudaError_t launch_2d_stream(int K, int kinds, const StreamLaunch& L, int j0, int nsteps, int grid, cudaStream_t s) {
@@ -704,10 +718,9 @@ cudaError_t launch_2d_stream(int K, int kinds, const StreamLaunch& L, int j0, in
   if (nsteps > 1 && (kinds != STREAM_EVEN || !L.dep_range || !L.deps || !L.flags || !L.wait_flag ||
                      (int64_t)L.n_items * nsteps > INT32_MAX))
     return cudaErrorInvalidValue;
-  if (K == 1) launch_s<1>(kinds, L, j0, nsteps, grid, s);
-  else if (K == 2) launch_s<2>(kinds, L, j0, nsteps, grid, s);
-  else return cudaErrorInvalidValue;
-  return cudaGetLastError();
+  if (K == 1) return launch_s<1>(kinds, L, j0, nsteps, grid, s);
+  if (K == 2) return launch_s<2>(kinds, L, j0, nsteps, grid, s);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t stream_dep_extra_set(unsigned extra) {
@@ -913,16 +926,14 @@ cudaError_t launch_2d_stage(int dtype, int n, int s, const void* src, void* u, c
   dim3 grid((n + 31) / 32, (n + 7) / 8);
   if (dtype == NLS_C128) {
     const Params<double> p = make_params<double>(ph, dt, op.center, op.w[0], op.w[1]);
-    if (op.K == 1) rk4_2d_stage<double, 1><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, p);
-    else if (op.K == 2) rk4_2d_stage<double, 2><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, p);
-    else return cudaErrorInvalidValue;
-  } else {
-    const Params<float> p = make_params<float>(ph, dt, op.center, op.w[0], op.w[1]);
-    if (op.K == 1) rk4_2d_stage<float, 1><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, p);
-    else if (op.K == 2) rk4_2d_stage<float, 2><<<grid, 256, 0, st>>>(n, s, src, u, P, acc, dst, p);
-    else return cudaErrorInvalidValue;
+    if (op.K == 1) return launch_pdl(rk4_2d_stage<double, 1>, grid, dim3(256), 0, st, n, s, src, u, P, acc, dst, p);
+    if (op.K == 2) return launch_pdl(rk4_2d_stage<double, 2>, grid, dim3(256), 0, st, n, s, src, u, P, acc, dst, p);
+    return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
+  const Params<float> p = make_params<float>(ph, dt, op.center, op.w[0], op.w[1]);
+  if (op.K == 1) return launch_pdl(rk4_2d_stage<float, 1>, grid, dim3(256), 0, st, n, s, src, u, P, acc, dst, p);
+  if (op.K == 2) return launch_pdl(rk4_2d_stage<float, 2>, grid, dim3(256), 0, st, n, s, src, u, P, acc, dst, p);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_rhs_2d(int dtype, int n, const void* u, const void* P, void* v, const PhysD& ph,

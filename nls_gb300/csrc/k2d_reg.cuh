@@ -256,6 +256,8 @@ rk4_2d_reg(const Inst2D* __restrict__ insts, const TileItem* __restrict__ items,
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int x0 = 2 * lane;  // region column of the pair's first node
   const int y0 = warp * NJ;
+  pdl_wait();      // the previous launch's states (programmatic launch)
+  pdl_trigger();
 
   // One tile: load this thread's rows (from the staging boxes or from global memory), run the
   // step, store the output rows.

@@ -242,6 +242,13 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
     if (lane == 0) v = atomicAdd(&counter[0], 1u);
     return (int)__shfl_sync(0xffffffffu, v, 0);
   };
+  // the previous launch's states and its reset of the counter first (programmatic launch; order 3
+  // only, where launches are short enough for it to matter: at order 5 the two instructions push
+  // the 255-register loop into spilling)
+  if (K == 1) {
+    pdl_wait();
+    pdl_trigger();
+  }
 
   const bool multi = nsteps > 1;
   // the flag index and value this warp publishes when its item is done (kept in shared memory,

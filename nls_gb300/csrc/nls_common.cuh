@@ -16,6 +16,31 @@
 
 namespace nlsg {
 
+// Programmatic dependent launch: a kernel launched with programmatic stream serialisation may
+// start while the kernel before it in the stream is still running.  pdl_wait() blocks until that
+// kernel has completed and its memory operations are visible (it returns at once when there is
+// no such predecessor), so it comes before anything reads the predecessor's output;
+// pdl_trigger() then lets the next kernel's CTAs be scheduled as this one's free their SMs.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+
+// Launch with programmatic stream serialisation (see pdl_wait).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 template <typename T> struct C2;
 template <> struct C2<float> { typedef float2 type; };
 template <> struct C2<double> { typedef double2 type; };
