@@ -841,15 +841,54 @@ int stream_choose_ly_search(const std::vector<int>& ns, int K, int64_t slots) {
   return best;
 }
 
-void stream_items(int inst, int n, int K, int ly, std::vector<StripItem>& out) {
+void stream_items(int inst, int n, int K, int ly, std::vector<StripItem>& out, int extra_strips) {
   std::vector<StripGeom> st;
-  std::vector<std::pair<int, int>> sg;
+  std::vector<std::pair<int, int>> sg, sg1;
   stream_strips(n, K, st);
   segments(n, ly, sg);
-  for (auto& g : st)
-    for (auto& y : sg)
-      out.push_back(StripItem{inst, (uint16_t)g.x0, (uint16_t)g.ox0, (uint16_t)g.ox1, (uint16_t)y.first,
+  // the first extra_strips strips are cut into one segment more
+  const int nseg = (int)sg.size();
+  for (int k = 0; k < nseg + 1; ++k) {
+    const int a = (int)((int64_t)k * n / (nseg + 1)), b = (int)((int64_t)(k + 1) * n / (nseg + 1));
+    if (b > a) sg1.emplace_back(a, b);
+  }
+  for (size_t q = 0; q < st.size(); ++q)
+    for (auto& y : ((int)q < extra_strips && nseg < n ? sg1 : sg))
+      out.push_back(StripItem{inst, (uint16_t)st[q].x0, (uint16_t)st[q].ox0, (uint16_t)st[q].ox1, (uint16_t)y.first,
                               (uint16_t)y.second, 0});
+}
+
+void stream_list_items(const std::vector<int>& ns, int K, int ly, int64_t slots, std::vector<StripItem>& out) {
+  // A list of fewer items than resident warps, short of them by no more than its strip count,
+  // takes exactly one item per warp: strips of the largest grids get one segment more.  Every SM
+  // then holds as many items as warps (an SM holding one item fewer than the others would finish
+  // its share early and idle while the rest finish theirs).
+  std::vector<StripGeom> st;
+  std::vector<std::pair<int, int>> sg;
+  std::vector<int> nstrips(ns.size()), extra(ns.size(), 0);
+  int64_t items = 0, strips = 0;
+  for (size_t k = 0; k < ns.size(); ++k) {
+    stream_strips(ns[k], K, st);
+    segments(ns[k], ly, sg);
+    nstrips[k] = (int)st.size();
+    items += (int64_t)st.size() * sg.size();
+    strips += (int64_t)st.size();
+  }
+  int64_t deficit = slots - items;
+  // order 3 only: at order 5 the extra segments' 16 rows of warm-up and drain each cost more than
+  // the balance gains (4096^2: 1.24e11 -> 1.20e11 node-steps/s; order 3: 2.17e11 -> 2.22e11)
+  if (K == 1 && deficit > 0 && deficit <= strips) {
+    std::vector<int> order(ns.size());
+    for (size_t k = 0; k < ns.size(); ++k) order[k] = (int)k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ns[a] > ns[b]; });
+    for (int k : order) {
+      const int take = (int)std::min<int64_t>(deficit, nstrips[k]);
+      extra[k] = take;
+      deficit -= take;
+      if (!deficit) break;
+    }
+  }
+  for (size_t k = 0; k < ns.size(); ++k) stream_items((int)k, ns[k], K, ly, out, extra[k]);
 }
 
 void stream_deps(const std::vector<StripItem>& items, const std::vector<int>& ns, int K, std::vector<int2>& range,
@@ -857,55 +896,33 @@ void stream_deps(const std::vector<StripItem>& items, const std::vector<int>& ns
   const int H = 4 * K;
   range.assign(items.size(), int2{0, 0});
   deps.clear();
-  // per instance: its strips (by x0) and segments (by y0), and the item at each (strip, segment)
-  std::map<int, std::vector<int>> by_inst;
-  for (size_t k = 0; k < items.size(); ++k) by_inst[items[k].inst].push_back((int)k);
+  // per instance and strip (by x0): its items; a strip's read and write columns only meet those of
+  // the strips within two of it, and segments may differ from strip to strip
+  std::map<int, std::map<int, std::vector<int>>> by;
+  for (size_t k = 0; k < items.size(); ++k) by[items[k].inst][items[k].x0].push_back((int)k);
   std::vector<std::vector<int>> lists(items.size());
-  for (auto& kv : by_inst) {
-    const int n = ns[kv.first];
-    std::vector<int> xs, ys;
-    for (int k : kv.second) {
-      xs.push_back(items[k].x0);
-      ys.push_back(items[k].y0);
-    }
-    std::sort(xs.begin(), xs.end());
-    xs.erase(std::unique(xs.begin(), xs.end()), xs.end());
-    std::sort(ys.begin(), ys.end());
-    ys.erase(std::unique(ys.begin(), ys.end()), ys.end());
-    std::vector<int> at(xs.size() * ys.size(), -1);
-    auto sx = [&](int x0) { return (int)(std::lower_bound(xs.begin(), xs.end(), x0) - xs.begin()); };
-    auto sy = [&](int y0) { return (int)(std::lower_bound(ys.begin(), ys.end(), y0) - ys.begin()); };
-    for (int k : kv.second) at[(size_t)sx(items[k].x0) * ys.size() + sy(items[k].y0)] = k;
-    // read region: the strip's columns and the segment's rows widened by the 4K-row warm-up and
-    // drain; written region: the output columns and the segment's rows
-    auto rows_r = [&](const StripItem& a, int& r0, int& r1) {
-      r0 = std::max(0, (int)a.y0 - H);
-      r1 = std::min(n, (int)a.y1 + H);
-    };
-    auto meets = [](int a0, int a1, int b0, int b1) { return a0 < b1 && b0 < a1; };
-    for (int k : kv.second) {
-      const StripItem& a = items[k];
-      int ar0, ar1;
-      rows_r(a, ar0, ar1);
-      const int s = sx(a.x0);
-      // candidate segments: those starting before the widened rows end, from the first one that
-      // may reach them
-      for (int s2 = std::max(0, s - 2); s2 <= std::min((int)xs.size() - 1, s + 2); ++s2) {
-        int g0 = (int)(std::upper_bound(ys.begin(), ys.end(), std::max(0, ar0 - 1)) - ys.begin()) - 1;
-        g0 = std::max(0, g0);
-        for (int g = g0; g < (int)ys.size() && ys[g] < ar1 + 1; ++g) {
-          const int d = at[(size_t)s2 * ys.size() + g];
-          if (d < 0) continue;
-          const StripItem& b = items[d];
-          int br0, br1;
-          rows_r(b, br0, br1);
-          const int ac1 = std::min(n, (int)a.x0 + 64), bc1 = std::min(n, (int)b.x0 + 64);
-          const bool raw = meets(ar0, ar1, b.y0, std::min(n, (int)b.y1)) && meets(a.x0, ac1, b.ox0, b.ox1);
-          const bool war = meets(br0, br1, a.y0, std::min(n, (int)a.y1)) && meets(b.x0, bc1, a.ox0, a.ox1);
-          if (raw || war) lists[k].push_back(d);
-        }
+  auto meets = [](int a0, int a1, int b0, int b1) { return a0 < b1 && b0 < a1; };
+  for (auto& inst : by) {
+    const int n = ns[inst.first];
+    std::vector<const std::vector<int>*> strips;
+    for (auto& kv : inst.second) strips.push_back(&kv.second);
+    for (size_t s = 0; s < strips.size(); ++s)
+      for (int k : *strips[s]) {
+        const StripItem& a = items[k];
+        // read region: the strip's columns and the segment's rows widened by the 4K-row warm-up
+        // and drain; written region: the output columns and the segment's rows
+        const int ar0 = std::max(0, (int)a.y0 - H), ar1 = std::min(n, (int)a.y1 + H);
+        const int ac1 = std::min(n, (int)a.x0 + 64);
+        for (size_t s2 = s >= 2 ? s - 2 : 0; s2 < std::min(strips.size(), s + 3); ++s2)
+          for (int d : *strips[s2]) {
+            const StripItem& b = items[d];
+            const int br0 = std::max(0, (int)b.y0 - H), br1 = std::min(n, (int)b.y1 + H);
+            const int bc1 = std::min(n, (int)b.x0 + 64);
+            const bool raw = meets(ar0, ar1, b.y0, std::min(n, (int)b.y1)) && meets(a.x0, ac1, b.ox0, b.ox1);
+            const bool war = meets(br0, br1, a.y0, std::min(n, (int)a.y1)) && meets(b.x0, bc1, a.ox0, a.ox1);
+            if (raw || war) lists[k].push_back(d);
+          }
       }
-    }
   }
   for (size_t k = 0; k < items.size(); ++k) {
     std::sort(lists[k].begin(), lists[k].end());

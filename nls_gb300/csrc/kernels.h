@@ -110,7 +110,10 @@ struct StripGeom {
 };
 void stream_strips(int n, int K, std::vector<StripGeom>& out);
 int stream_choose_ly(const std::vector<int>& ns, int K, int64_t slots);
-void stream_items(int inst, int n, int K, int ly, std::vector<StripItem>& out);
+void stream_items(int inst, int n, int K, int ly, std::vector<StripItem>& out, int extra_strips = 0);
+// The items of a list of grids at segment height ly for `slots` resident warps (see the
+// definition: lists just short of one item per warp are topped up to exactly one).
+void stream_list_items(const std::vector<int>& ns, int K, int ly, int64_t slots, std::vector<StripItem>& out);
 void stream_sort_items(std::vector<StripItem>& items);
 // Dependency lists of a sorted item list (ns: grid side by instance): for item k every item of the
 // same instance whose written region meets k's read region, or whose read region meets k's written

@@ -317,7 +317,7 @@ static int solve_2d_stream(nls_ctx* ctx, const nls_problem* pr, const Stencil2D&
   I.steps = INT64_MAX; I.dt = pr->dt; I.ph = ph; I.op = op;
   set_params(I);
   std::vector<StripItem> items;
-  stream_items(0, n, op.K, stream_plan_ly(ctx, {n}, op.K), items);
+  stream_list_items({n}, op.K, stream_plan_ly(ctx, {n}, op.K), stream_slots(ctx, op.K), items);
   stream_sort_items(items);
   const int kinds = stream_kind(n, I.u[0], I.u[1], P);
   const int n_items = (int)items.size();
@@ -749,7 +749,7 @@ static int batch_build(nls_batch* b, const nls_problem* probs, int count) {
       for (int i : G.idx) ns.push_back(b->m[i].pr.n);
       const int ly = stream_plan_ly(ctx, ns, G.K);
       G.sitems_h.clear();
-      for (size_t k = 0; k < G.idx.size(); ++k) stream_items((int)k, ns[k], G.K, ly, G.sitems_h);
+      stream_list_items(ns, G.K, ly, stream_slots(ctx, G.K), G.sitems_h);
       stream_sort_items(G.sitems_h);
       stream_deps(G.sitems_h, ns, G.K, G.range_h, G.deps_h);
       items = (int)G.sitems_h.size();
@@ -1616,7 +1616,7 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
         std::vector<int> ns;
         for (int i : kv.second) ns.push_back(p->slots[i].pr.n);
         const int ly = stream_plan_ly(ctx, ns, K);
-        for (size_t k = 0; k < ns.size(); ++k) stream_items((int)k, ns[k], K, ly, sitems[gi]);
+        stream_list_items(ns, K, ly, stream_slots(ctx, K), sitems[gi]);
         stream_sort_items(sitems[gi]);
         stream_deps(sitems[gi], ns, K, sranges[gi], sdeps[gi]);
       }
