@@ -599,8 +599,79 @@ static cudaError_t launch_reg1d(const Inst1D* d, int count, int seg_cap, cudaStr
   return cudaErrorInvalidValue;
 }
 
+// Complex64 over a cluster: the register-resident cluster kernel, one segment and its halos per
+// CTA (NPT as for one CTA: 8 in a launch of many grids, else the smallest that fits 512 threads).
+template <int K>
+static cudaError_t launch_reg1d_cl(const Inst1D* d, int count, int cl, int seg_cap, cudaStream_t s,
+                                   bool prepare_only) {
+  const int nodes = seg_cap + 8 * K;
+  int npt = 1;
+  while (npt < K) npt *= 2;
+  while (npt * 512 < nodes) npt *= 2;
+  if (count > 1) npt = 8;
+  if (!prepare_only && (npt > 8 || npt < K || npt * 512 < nodes)) return cudaErrorInvalidValue;
+  npt = std::min(npt, 8);
+  int nt = (nodes + npt - 1) / npt;
+  nt = ((nt + 31) / 32) * 32;
+  const size_t smem = ((size_t)2 * (nt / 32) * 2 * K + (size_t)2 * 2 * 4 * K) * sizeof(float2);
+  auto launch = [&](auto kern) -> cudaError_t {
+    static bool non_portable = false;
+    if (cl > 8 && !non_portable) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      if (e != cudaSuccess) return e;
+      non_portable = true;
+    }
+    if (prepare_only) return cudaSuccess;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(count * cl);
+    cfg.blockDim = dim3(nt);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, d, cl);
+  };
+  if (prepare_only) {
+    // a later launch may take any nodes-per-thread form (one grid: the smallest that fits; many
+    // grids: 8): prepare them all
+    cudaError_t e = cudaSuccess;
+    if (K <= 1) e = launch(rk4_1d_reg_cl<(K <= 1 ? K : 1), 1>);
+    if (!e && K <= 2) e = launch(rk4_1d_reg_cl<(K <= 2 ? K : 2), 2>);
+    if (!e) e = launch(rk4_1d_reg_cl<K, 4>);
+    if (!e) e = launch(rk4_1d_reg_cl<K, 8>);
+    return e;
+  }
+  switch (npt) {
+    case 1: if (K <= 1) return launch(rk4_1d_reg_cl<(K <= 1 ? K : 1), 1>);
+            return cudaErrorInvalidValue;
+    case 2: if (K <= 2) return launch(rk4_1d_reg_cl<(K <= 2 ? K : 2), 2>);
+            return cudaErrorInvalidValue;
+    case 4: return launch(rk4_1d_reg_cl<K, 4>);
+    case 8: return launch(rk4_1d_reg_cl<K, 8>);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// Portable cluster sizes only: 16-CTA clusters of this kernel failed to launch inside a batch's
+// graph capture (cudaErrorInvalidClusterSize) although they launch directly; they keep the
+// shared-memory cluster kernel.
+bool reg1d_cluster_fits(int K, int cl, int seg_cap, int shortest_seg) {
+  return cl > 1 && cl <= 8 && shortest_seg >= 4 * K && seg_cap + 8 * K <= 512 * 8;
+}
+
 static cudaError_t dispatch_res(int dtype, int K, const Inst1D* d_insts, int count, int cl,
-                                int seg_cap, cudaStream_t s, bool prepare_only) {
+                                int seg_cap, int shortest_seg, cudaStream_t s, bool prepare_only) {
+  if (dtype == NLS_C64 && reg1d_cluster_fits(K, cl, seg_cap, shortest_seg)) {
+    if (K == 1) return launch_reg1d_cl<1>(d_insts, count, cl, seg_cap, s, prepare_only);
+    if (K == 2) return launch_reg1d_cl<2>(d_insts, count, cl, seg_cap, s, prepare_only);
+    if (K == 3) return launch_reg1d_cl<3>(d_insts, count, cl, seg_cap, s, prepare_only);
+    return cudaErrorInvalidValue;
+  }
   if (dtype == NLS_C64 && cl == 1) {
     if (K == 1) return launch_reg1d<1>(d_insts, count, seg_cap, s, prepare_only);
     if (K == 2) return launch_reg1d<2>(d_insts, count, seg_cap, s, prepare_only);
@@ -623,14 +694,17 @@ int resident_1d_seg_limit(int dtype) { return dtype == NLS_C128 ? 2048 : 4096; }
 
 cudaError_t prepare_1d_resident(int dtype, int K, int cl, int seg_cap) {
   if (seg_cap > resident_1d_seg_limit(dtype) || cl < 1 || cl > 16) return cudaErrorInvalidValue;
-  return dispatch_res(dtype, K, nullptr, 0, cl, seg_cap, nullptr, true);
+  cudaError_t e = dispatch_res(dtype, K, nullptr, 0, cl, seg_cap, 0, nullptr, true);
+  if (e == cudaSuccess && dtype == NLS_C64 && reg1d_cluster_fits(K, cl, seg_cap, 4 * K))
+    e = dispatch_res(dtype, K, nullptr, 0, cl, seg_cap, 4 * K, nullptr, true);
+  return e;
 }
 
 cudaError_t launch_1d_resident(int dtype, int K, const Inst1D* d_insts, int count, int cl,
-                               int seg_cap, cudaStream_t s) {
+                               int seg_cap, int shortest_seg, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   if (seg_cap > resident_1d_seg_limit(dtype) || cl < 1 || cl > 16) return cudaErrorInvalidValue;
-  return dispatch_res(dtype, K, d_insts, count, cl, seg_cap, s, false);
+  return dispatch_res(dtype, K, d_insts, count, cl, seg_cap, shortest_seg, s, false);
 }
 
 template <typename T, int K>

@@ -163,4 +163,91 @@ __global__ void __launch_bounds__(512) rk4_1d_reg(const Inst1D* __restrict__ ins
     if (p0 + i < n) Uo[p0 + i] = u[i];
 }
 
+// Cluster form (grids too long for one CTA): the grid is cut into cl segments [q0, q1), one per
+// CTA of a thread-block cluster.  Each CTA holds its segment and up to H = 4K halo nodes on either
+// side, [lo, hi), in registers with the single-CTA layout above, and runs the four stages over all
+// of them with CTA-local barriers only; a node within K of [lo, hi)'s ends reads zeros past them,
+// so after stage s the values within sK of those ends are wrong, and after the four stages exactly
+// the segment itself is exact.  At the end of each step every CTA pushes the H new values at
+// either end of its segment into its neighbours' halo buffers (distributed shared memory, double
+// buffered by step parity: a buffer written at step s is read at the start of step s + 1 and
+// written again only after the cluster's next meeting) and the cluster meets once; the next step
+// starts by taking its halo nodes from those buffers.  Every CTA runs the same loop with no early
+// exit, so the cluster's barriers always match.
+template <int K, int NPT>
+__global__ void __launch_bounds__(512) rk4_1d_reg_cl(const Inst1D* __restrict__ insts, int cl) {
+  static_assert(NPT >= K, "a thread's neighbours must lie within the adjacent lanes");
+  constexpr int H = 4 * K;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  float2* ex = reinterpret_cast<float2*>(smem_raw);   // [2 parities][warps][2 ends][K]
+  float2* halo = ex + 2 * nw * 2 * K;                 // [2 parities][2 sides: left, right][H]
+  cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
+  const int inst = blockIdx.x / cl, rank = blockIdx.x % cl;
+  const Inst1D& I = insts[inst];
+  const int n = I.n;
+  const int seg = (n + cl - 1) / cl;
+  const int q0 = min(n, rank * seg), q1 = min(n, q0 + seg);
+  const int lo = max(0, q0 - H), hi = min(n, q1 + H);
+  const int p0 = lo + tid * NPT;
+  const Reg1DConst<K> c = reg1d_const<K>(I);
+  const float h = (float)I.op.h;
+  const float c12 = I.pf.c12;
+  const float2* __restrict__ Ug = reinterpret_cast<const float2*>(I.u);
+  const float* __restrict__ Pg = reinterpret_cast<const float*>(I.P);
+  float2 u[NPT], t[NPT], acc[NPT];
+  float pc[NPT], ir[NPT];
+#pragma unroll
+  for (int i = 0; i < NPT; ++i) {
+    const int p = p0 + i;
+    const bool in = p < hi;
+    u[i] = in ? Ug[p] : f2(0.f, 0.f);
+    pc[i] = in ? c12 * Pg[p] : 0.f;
+    ir[i] = p >= K ? 1.f / ((float)p * h) : 0.f;
+    acc[i] = f2(0.f, 0.f);
+  }
+  // the neighbours' halo buffers (their right side takes this segment's first H nodes, their
+  // left side its last H)
+  float2* const lnb = rank > 0 ? cluster.map_shared_rank(halo, rank - 1) : nullptr;
+  float2* const rnb = rank < cl - 1 ? cluster.map_shared_rank(halo, rank + 1) : nullptr;
+  cluster.sync();   // every CTA of the cluster is running before the first push
+  float2 L[K], R[K];
+  const int64_t steps = I.steps;
+  for (int64_t step = 0; step < steps; ++step) {
+    const int par = (int)(step & 1);
+    if (step > 0) {
+      const float2* hb = halo + (par ^ 1) * 2 * H;
+#pragma unroll
+      for (int i = 0; i < NPT; ++i) {
+        const int p = p0 + i;
+        if (p >= lo && p < q0) u[i] = hb[p - (q0 - H)];
+        if (p >= q1 && p < hi) u[i] = hb[H + (p - q1)];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < NPT; ++i) t[i] = u[i];
+    reg1d_halo<K, NPT, 1>(t, L, R, ex, warp, lane, nw);
+    reg1d_stage<K, NPT, 1>(t, acc, u, pc, ir, L, R, p0, hi, c);
+    reg1d_halo<K, NPT, 2>(t, L, R, ex, warp, lane, nw);
+    reg1d_stage<K, NPT, 2>(t, acc, u, pc, ir, L, R, p0, hi, c);
+    reg1d_halo<K, NPT, 3>(t, L, R, ex, warp, lane, nw);
+    reg1d_stage<K, NPT, 3>(t, acc, u, pc, ir, L, R, p0, hi, c);
+    reg1d_halo<K, NPT, 4>(t, L, R, ex, warp, lane, nw);
+    reg1d_stage<K, NPT, 4>(t, acc, u, pc, ir, L, R, p0, hi, c);
+#pragma unroll
+    for (int i = 0; i < NPT; ++i) {
+      const int p = p0 + i;
+      if (lnb && p >= q0 && p < q0 + H) lnb[(par * 2 + 1) * H + (p - q0)] = u[i];
+      if (rnb && p >= q1 - H && p < q1) rnb[(par * 2 + 0) * H + (p - (q1 - H))] = u[i];
+    }
+    cluster.sync();
+  }
+  float2* __restrict__ Uo = reinterpret_cast<float2*>(I.u);
+#pragma unroll
+  for (int i = 0; i < NPT; ++i) {
+    const int p = p0 + i;
+    if (p >= q0 && p < q1) Uo[p] = u[i];
+  }
+}
+
 }  // namespace nlsg

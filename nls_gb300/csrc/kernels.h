@@ -19,8 +19,16 @@ namespace nlsg {
 int resident_1d_seg_limit(int dtype);
 // Sets the kernel attributes a later launch with these parameters needs (call outside capture).
 cudaError_t prepare_1d_resident(int dtype, int K, int cl, int seg_cap);
+// shortest_seg: the shortest of the cl segments over the launch's grids (see shortest_segment);
+// complex64 clusters take the register-resident cluster kernel when every segment holds at least
+// the 4K halo nodes a neighbour needs and a segment with its halos fits one CTA.
 cudaError_t launch_1d_resident(int dtype, int K, const Inst1D* d_insts, int count, int cl,
-                               int seg_cap, cudaStream_t s);
+                               int seg_cap, int shortest_seg, cudaStream_t s);
+// The last (shortest) of the segments a grid of n nodes is cut into for cl CTAs of ceil(n / cl).
+inline int shortest_segment(int n, int cl) {
+  const int seg = (n + cl - 1) / cl;
+  return n - (cl - 1) * seg;
+}
 cudaError_t launch_1d_stage(int dtype, int n, int s, const void* src, void* u, const void* P,
                             void* acc, void* dst, double dt, const PhysD& ph, const Stencil1D& op,
                             cudaStream_t st);

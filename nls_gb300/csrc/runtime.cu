@@ -225,7 +225,8 @@ static int solve_1d_dev(nls_ctx* ctx, int dtype, const nls_problem* pr, int64_t 
     CK(ctx, ctx->desc.ensure(sizeof(Inst1D)));
     CK(ctx, cudaMemcpyAsync(ctx->desc.p, &I, sizeof(I), cudaMemcpyHostToDevice, ctx->stream));
     const int seg = (n + cl - 1) / cl;
-    CK(ctx, launch_1d_resident(dtype, op.K, (const Inst1D*)ctx->desc.p, 1, cl, seg, ctx->stream));
+    CK(ctx, launch_1d_resident(dtype, op.K, (const Inst1D*)ctx->desc.p, 1, cl, seg, shortest_segment(n, cl),
+                               ctx->stream));
     ctx->launches += 1;
     return NLS_OK;
   }
@@ -892,7 +893,10 @@ static cudaError_t batch_sequence(nls_batch* b, int64_t steps) {
       if ((e = cudaStreamWaitEvent(ctx->side[i], ctx->ev_fork, 0))) return e;
     for (size_t g = 0; g < b->g1.size(); ++g) {
       auto& G = b->g1[g];
-      if ((e = launch_1d_resident(dtype, G.K, G.d, (int)G.idx.size(), G.cl, G.seg_cap, ctx->side[g % nside])))
+      int shortest = INT32_MAX;
+      for (int i : G.idx) shortest = std::min(shortest, shortest_segment(b->m[i].pr.n, G.cl));
+      if ((e = launch_1d_resident(dtype, G.K, G.d, (int)G.idx.size(), G.cl, G.seg_cap, shortest,
+                                  ctx->side[g % nside])))
         return e;
     }
   }
@@ -1645,14 +1649,14 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
   p->h_desc.assign(bytes, 0);
   CK(ctx, p->d_desc[buf].ensure(bytes));
   char* d = (char*)p->d_desc[buf].p;
-  struct L1 { int K, cl, seg, count; size_t off; };
+  struct L1 { int K, cl, seg, shortest, count; size_t off; };
   struct L2 { int K, shape, n_items, grid; size_t off, off_items; StreamListLayout ly; bool tma; int kinds; };
   std::vector<L1> l1;
   std::vector<L2> l2;
   size_t off = 0;
   for (auto& kv : g1) {
     Inst1D* h = (Inst1D*)(p->h_desc.data() + off);
-    int seg = 0;
+    int seg = 0, shortest = INT32_MAX;
     for (size_t k = 0; k < kv.second.size(); ++k) {
       const Slot& S = p->slots[kv.second[k]];
       Inst1D& I = h[k];
@@ -1661,8 +1665,9 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
       I.dt = S.pr.dt; I.ph = phys_of(S.pr.coeffs); I.op = S.op1;
       set_params(I);
       seg = std::max(seg, (S.pr.n + S.cl - 1) / S.cl);
+      shortest = std::min(shortest, shortest_segment(S.pr.n, S.cl));
     }
-    l1.push_back(L1{kv.first.first, kv.first.second, seg, (int)kv.second.size(), off});
+    l1.push_back(L1{kv.first.first, kv.first.second, seg, shortest, (int)kv.second.size(), off});
     off += align256(sizeof(Inst1D) * kv.second.size());
   }
   size_t gi = 0;
@@ -1722,7 +1727,7 @@ static int pool_launch_locked(nls_pool* p, int* launched) {
     CK(ctx, cudaEventRecord(ctx->ev_fork, ctx->stream));
     CK(ctx, cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0));
     for (auto& L : l1) {
-      CK(ctx, launch_1d_resident(dtype, L.K, (const Inst1D*)(d + L.off), L.count, L.cl, L.seg, ctx->aux));
+      CK(ctx, launch_1d_resident(dtype, L.K, (const Inst1D*)(d + L.off), L.count, L.cl, L.seg, L.shortest, ctx->aux));
       ctx->launches += 1;
     }
   }
