@@ -45,14 +45,16 @@ typedef struct nls_pool nls_pool;
 
 /* One solve: dim 1 is the radial 1-D model of solve_nls (nls/nls.f90:797-813), dim 2 the
  * Cartesian model of solve_nls_2d (nls/nls.f90:903-919).  variant selects a kernel shape chosen by
- * the autotuner (-1 = built-in choice): 1-D = CTAs per solve (cluster size 1..16; 1 runs the
- * register-resident kernel for complex64; 0 = unfused stage kernels); 2-D = 0 unfused, or a fused tile region (threads): 1 = 64x64 (512),
+ * the autotuner (-1 = built-in choice): 1-D = CTAs per solve (cluster size 1..16; complex64 runs
+ * the register-resident kernel on 1 CTA and its cluster form on 2..8 CTAs whenever each segment
+ * holds at least 4K nodes; 0 = unfused stage kernels); 2-D = 0 unfused, or a fused tile region (threads): 1 = 64x64 (512),
  * 2 = 128x32 (512), 3 = 32x32 (256), 4 = 64x64 (1024), 5 = 128x32 (1024),
  * 6 = 64 x (64 + 8K) with output tiles exactly 64 rows high (512), 7 = the same region with 768
  * (order 3) or 640 (order 5) threads; register-resident tiles (complex64 only), region 64 wide:
  * 8 = 64x80 (512), 9 = 64x96 (384), 10 = 64x96 (256), 11 = 64x64 (512), 12 = 64x72 (256),
  * 13 = 64x72 (384), 14 = 64x80 (256); 15 = streaming wavefront over 64-column strips (complex64
- * only; the complex64 default). */
+ * only; the complex64 default except order 5 below 2048 per side; order-3 work lists of at least
+ * 1.5 strip items per resident warp run up to 512 RK4 steps per launch). */
 typedef struct nls_problem {
   int dim;
   int n;

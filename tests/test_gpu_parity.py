@@ -563,6 +563,29 @@ def test_stream_dependency_wait_timeout_is_reported_and_the_context_recovers(gpu
     assert rel(got, want) <= 3e-5
 
 
+@pytest.mark.parametrize("order", [3, 5])
+def test_2d_c64_stream_4096_full_size(gpu, oracle_lib, order):
+    """A 4096^2 grid on the streaming step at full size: at order 3 its work list is topped up to
+    exactly one item per resident warp (strips of different segment counts), and launches follow
+    each other as programmatic dependent launches; against the FP32 oracle."""
+    s = _spec_2d(4096, order)
+    iters = 6
+    want32 = oracle_lib.solve(s.dt, s.dx, order, iters, s.pumping, s.coeffs, s.u0, dtype=np.float32,
+                              threads=os.cpu_count() or 1)
+    got = _device_solve(gpu, s, iters, np.complex64, 15)
+    assert rel(got, want32) <= 3e-5
+
+
+def test_1d_c64_register_cluster_single_solve(gpu, oracle_lib):
+    """An 8192-node radial grid alone on the register-resident cluster kernel (default cluster
+    size) against the FP32 oracle."""
+    s = _spec_1d(8192, 5)
+    iters = 500
+    want32 = oracle_lib.solve(s.dt, s.dx, 5, iters, s.pumping, s.coeffs, s.u0, dtype=np.float32)
+    got = _device_solve(gpu, s, iters, np.complex64, -1)
+    assert rel(got, want32) <= 3e-5
+
+
 @pytest.mark.parametrize("order,n", [(3, 1000), (5, 1000), (3, 1030), (5, 515)])
 def test_2d_c64_stream_large_grids(gpu, oracle_lib, order, n):
     """The streaming step on grids of many strips and row segments (segment warm-up and drain,
