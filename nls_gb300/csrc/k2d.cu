@@ -841,6 +841,30 @@ int stream_choose_ly_search(const std::vector<int>& ns, int K, int64_t slots) {
   return best;
 }
 
+int stream_choose_ly_multi(const std::vector<int>& ns, int K, int64_t slots, double items_per_slot, int min_ly) {
+  // the tallest segment (least warm-up and drain) whose items still number items_per_slot per
+  // resident warp; -1 when that needs segments below min_ly rows
+  int nmax = 1;
+  std::vector<int> nstrips(ns.size());
+  std::vector<StripGeom> st;
+  for (size_t k = 0; k < ns.size(); ++k) {
+    nmax = std::max(nmax, ns[k]);
+    stream_strips(ns[k], K, st);
+    nstrips[k] = (int)st.size();
+  }
+  std::vector<std::pair<int, int>> sg;
+  for (int seg = 1;; ++seg) {
+    const int ly = (nmax + seg - 1) / seg;
+    if (ly < min_ly) return -1;
+    int64_t items = 0;
+    for (size_t k = 0; k < ns.size(); ++k) {
+      segments(ns[k], ly, sg);
+      items += (int64_t)sg.size() * nstrips[k];
+    }
+    if ((double)items >= items_per_slot * (double)slots) return ly;
+  }
+}
+
 void stream_items(int inst, int n, int K, int ly, std::vector<StripItem>& out, int extra_strips) {
   std::vector<StripGeom> st;
   std::vector<std::pair<int, int>> sg, sg1;

@@ -118,6 +118,9 @@ struct StripGeom {
 };
 void stream_strips(int n, int K, std::vector<StripGeom>& out);
 int stream_choose_ly(const std::vector<int>& ns, int K, int64_t slots);
+// The tallest segment height giving at least items_per_slot items per resident warp, or -1 if
+// that needs segments below min_ly rows.
+int stream_choose_ly_multi(const std::vector<int>& ns, int K, int64_t slots, double items_per_slot, int min_ly);
 void stream_items(int inst, int n, int K, int ly, std::vector<StripItem>& out, int extra_strips = 0);
 // The items of a list of grids at segment height ly for `slots` resident warps (see the
 // definition: lists just short of one item per warp are topped up to exactly one).

@@ -277,11 +277,23 @@ static constexpr int kStreamStepsPerLaunch = 512;
 static std::atomic<int> g_stream_multi_mode{0};   // test control: 0 automatic, 1 always, 2 never
 
 // Segment height of a streaming list over grids ns: the one-step-per-launch schedule simulation's
-// choice.  (Choosing instead the tallest height that gives 1.5 items per warp, so that single
-// large grids also run several steps per launch, measured: 4096^2 2.15e11 -> 2.18e11, 8192^2
-// 2.37e11 -> 2.13e11, the batched mix 2.23e11 -> 2.08e11 node-steps/s.)
+// choice, except for the largest lists (below).  (The tallest height giving only 1.5 items per
+// warp, so that more lists run several steps per launch, measured worse: 8192^2 2.37e11 ->
+// 2.13e11, the batched mix 2.23e11 -> 2.08e11; shorter segments on a 4096^2 grid, 2.21e11 ->
+// 2.15e11 at half the height and 2.05e11 at a third.)
 static int stream_plan_ly(nls_ctx* ctx, const std::vector<int>& ns, int K) {
-  return stream_choose_ly(ns, K, stream_slots(ctx, K));
+  const int64_t slots = stream_slots(ctx, K);
+  // Lists large enough for three items per resident warp at segments of 192 rows or more take
+  // the tallest such segments and run several steps per launch (the dataflow balances three
+  // items per warp; the warm-up and drain of segments that tall cost little): 8192^2 order 3
+  // 2.36e11 -> 2.44e11 node-steps/s.
+  bool paired = true;
+  for (int n : ns) paired = paired && n % 2 == 0;
+  if (K == 1 && paired && g_stream_multi_mode.load() != 2) {
+    const int ly = stream_choose_ly_multi(ns, K, slots, 3.0, 192);
+    if (ly > 0) return ly;
+  }
+  return stream_choose_ly(ns, K, slots);
 }
 static bool stream_multi_ok(nls_ctx* ctx, int K, int kinds, int n_items) {
   if (kinds != STREAM_EVEN || n_items <= 0) return false;
