@@ -658,8 +658,8 @@ static cudaError_t launch_reg1d_cl(const Inst1D* d, int count, int cl, int seg_c
 }
 
 // Portable cluster sizes only: 16-CTA clusters of this kernel failed to launch inside a batch's
-// graph capture (cudaErrorInvalidClusterSize) although they launch directly; they keep the
-// shared-memory cluster kernel.
+// graph capture (cudaErrorInvalidClusterSize; the profiler reports a maximum potential cluster
+// size of 8 for it); they keep the shared-memory cluster kernel.
 bool reg1d_cluster_fits(int K, int cl, int seg_cap, int shortest_seg) {
   return cl > 1 && cl <= 8 && shortest_seg >= 4 * K && seg_cap + 8 * K <= 512 * 8;
 }
