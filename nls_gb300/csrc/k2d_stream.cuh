@@ -275,7 +275,9 @@ rk4_2d_stream(const Inst2D* __restrict__ insts, const StripItem* __restrict__ it
         while (true) {
           const bool ok = d < 0 || (int)(ld_acquire_gpu(&flags[d]) - need) >= 0;
           if (__all_sync(0xffffffffu, ok)) break;
-          if (*reinterpret_cast<volatile int*>(wait_flag)) break;   // another warp timed out
+          // another warp timed out (decided for the whole warp: lanes may read the word at
+          // different moments)
+          if (__any_sync(0xffffffffu, *reinterpret_cast<volatile int*>(wait_flag) != 0)) break;
           if (++polls >= NLSG_STREAM_WAIT_POLLS) {
             if (lane == 0) atomicExch(wait_flag, 1);
             break;
