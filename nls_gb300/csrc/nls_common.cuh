@@ -70,11 +70,16 @@ template <typename T> __device__ __forceinline__ Phys<T> phys_of(const Params<T>
 // Division in the reservoir term.  Double precision: the FP64 pipe runs at a small fraction of
 // the FP32 rate on GB300, so the quotient is formed as a * (1/b) with the reciprocal computed by
 // the Newton-Raphson iteration y <- y + y (1 - b y) (each step squares the relative error) from an
-// FP32 seed (PTX rcp.approx.ftz.f32, relative error below 2^-22): two steps reach double
-// precision, and the quotient is within a few units in the last place of a / b.  Denominators
-// outside the FP32 normal range (and NaN) take the IEEE division.  Single precision (the precision
-// form) uses the hardware fast reciprocal-based quotient, within 2 ulp and far inside the form's
-// 1e-4 error budget.
+// FP32 seed (PTX rcp.approx.ftz.f32 of b rounded to float, relative error below about 2^-21 against
+// 1/b): one step leaves a relative error below about 2^-42 (2e-13), far inside the plain path's
+// 1e-10 parity over tens of thousands of steps, and saves two FP64 FMAs a node-stage against two
+// steps (configs 0 and 1: 5.46 -> 5.21 and 24.5 -> 23.4 us per step).  Denominators outside the
+// FP32 normal range (and NaN) take the IEEE division.  Single precision (the precision form)
+// uses the hardware fast reciprocal-based quotient, within 2 ulp and far inside the form's 1e-4
+// error budget.
+#ifndef NLSG_RDIV_NEWTON
+#define NLSG_RDIV_NEWTON 1
+#endif
 __device__ __forceinline__ double rdiv(double a, double b) {
   const float bf = (float)b;
   if (!(fabsf(bf) >= 1e-30f && fabsf(bf) <= 1e30f)) return a / b;
@@ -82,7 +87,7 @@ __device__ __forceinline__ double rdiv(double a, double b) {
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(s) : "f"(bf));
   double y = (double)s;
   y = __fma_rn(y, __fma_rn(-b, y, 1.0), y);
-  y = __fma_rn(y, __fma_rn(-b, y, 1.0), y);
+  if (NLSG_RDIV_NEWTON > 1) y = __fma_rn(y, __fma_rn(-b, y, 1.0), y);
   return a * y;
 }
 __device__ __forceinline__ float rdiv(float a, float b) { return __fdividef(a, b); }
