@@ -518,6 +518,35 @@ def test_batch_stream_schedules_match_single_solves(gpu, stream_mode, mode):
         assert np.array_equal(b.get(i), want), i
 
 
+def test_batch_and_pool_stream_mixed_forms_match_single_solves(gpu):
+    """Square grids of odd and even sides in one streaming group (both the paired and the per-node
+    form launch every step, over one work list) in a batch and in the pool equal single solves."""
+    from nls_gb300.batch import BatchSolver
+    from nls_gb300.serve import Pool
+    specs = []
+    for k, n in enumerate((64, 97, 130, 33, 256, 121)):
+        s = _spec_2d(n, 3, seed=40 + k)
+        s.variant = 15
+        specs.append(s)
+    b = BatchSolver(specs, dtype=np.complex64)
+    b.run(23)
+    pool = Pool(budget_bytes=1 << 30, chunk_steps=10)
+    for tag, s in enumerate(specs):
+        pool.admit(s, 23 + tag, tag)
+    got = {}
+    while True:
+        r = pool.take_with_state()
+        if r is not None:
+            got[r[0]] = r[1]
+            continue
+        if pool.status()[0] == 0:
+            break
+        pool.step()
+    for i, s in enumerate(specs):
+        assert np.array_equal(b.get(i), _device_solve(gpu, s, 23, np.complex64, 15)), i
+        assert np.array_equal(got[i], _device_solve(gpu, s, 23 + i, np.complex64, 15)), i
+
+
 def test_pool_stream_several_steps_per_launch_match_single_solves(gpu, stream_mode):
     """Pool chunks of the streaming kernel with several steps per launch, requests of different
     step counts (a request stops at its own count inside a launch), equal single solves."""
