@@ -196,9 +196,9 @@ struct StreamWin {
 // moves as one 16-byte copy (state) and one 8-byte copy (pump) and is stored as one 16-byte store;
 // otherwise every node moves on its own.  Items of the other kind are skipped (the runtime
 // launches both instantiations over the same item list when a group mixes them).
-// Register cap a thread.  Order 3: 152, so 13 one-warp CTAs fit an SM's 64K registers (the 5-row
-// window fits without spilling; a minimum-blocks bound of 13 would make the compiler aim for 128
-// and spill); order 5: 255 (8 one-warp CTAs per SM).
+// Register cap a thread.  Order 3: 152 (the 5-row window fits without spilling; registers are
+// allocated per SM sub-partition, so caps from 129 to 168 all give 3 warps per scheduler, 12 one-
+// warp CTAs per SM, and 128, for 16, spills); order 5: 255 (8 one-warp CTAs per SM).
 #ifndef NLSG_STREAM_MAXNREG_K1
 #define NLSG_STREAM_MAXNREG_K1 152
 #endif
